@@ -1,0 +1,261 @@
+/*
+ * sge.h — C ABI of the GB300 subgraph-enumeration executor (libsge.so).
+ *
+ * The library replaces the execution half of the reference's
+ * `graph_mining_system`: everything after the plan hand-off
+ * (main.cpp:64-86 serial, main.cpp:171-193 OpenMP), i.e. the calls
+ *   sharedJoin(t, pt, query, cs, trieLevels, visited, result, count, ...)
+ *       (matching/join.h:39-41, matching/join.cpp:812-1200)
+ *   parSharedJoin(t, pt, query, [DataGraph g,] cs, trieLevels, visited, result, count, traverse)
+ *       (matching/parallel.h:88-94, matching/parallel.cpp:1154-1844)
+ * and the data structures those read: the CSR data graph
+ * (relation/graph.h:113-213), the candidate-space accessors of unlabeled mode
+ * (relation/candidate_space.cpp:763-799) and the plan facts produced by
+ * plan/optimizer.cpp + plan/decomposition.cpp (flattened into sge_plan_blob).
+ *
+ * Conventions
+ *  - Every entry point returns an sge_status; on failure sge_last_error()
+ *    returns a one-line message (thread-local).  The library never calls exit().
+ *  - Vertex ids and CSR offsets are uint32 (the reference's VertexID/EdgeID,
+ *    config/config.h:42-44); counts are uint64 and wrap like the reference's
+ *    size_t accumulator.
+ *  - Handles are not thread-safe; calls are stream-ordered on one internal
+ *    CUDA stream per graph handle.
+ *  - No torch types, no C++ types: plain pointers and sizes only.
+ */
+#ifndef SGE_H
+#define SGE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SGE_ABI_VERSION 1u
+#define SGE_MAX_K 16u          /* pattern vertices supported by the device executor */
+#define SGE_MAX_TAIL 4u        /* levels counted (not enumerated) at the leaf */
+#define SGE_MAX_PARTITIONS 15u /* set partitions of a 4-vertex tail (Bell(4)) */
+#define SGE_PLAN_MAGIC 0x4E4C5053u /* "SPLN" */
+
+typedef enum sge_status {
+    SGE_OK = 0,
+    SGE_BAD_INPUT = 1,      /* malformed graph/pattern/plan/argument */
+    SGE_OOM = 2,            /* host or device allocation failed */
+    SGE_TIMEOUT = 3,        /* a launch exceeded its time budget (partial count kept) */
+    SGE_STACK_OVERFLOW = 4, /* a per-warp buffer would have overflowed (never silently) */
+    SGE_CUDA_ERROR = 5,     /* a CUDA runtime call failed */
+    SGE_UNSUPPORTED = 6,    /* pattern/plan shape outside the executor's limits */
+    SGE_IO_ERROR = 7,       /* file could not be opened or was truncated */
+    SGE_NO_DEVICE = 8       /* no CUDA device visible */
+} sge_status;
+
+/* Leaf counting modes (how the last tail_len levels are counted without
+ * enumerating them).  They restate the reference's traverse() variants,
+ * matching/join.cpp:1520-1691:
+ *   SINGLE  = TrieLevel::numResults on one last level (relation/relation.cpp:301-338)
+ *   CHOOSE  = symmLastLevel: choosec(num, r)              (join.cpp:1534-1538, utils.cpp:80-94)
+ *   IEP     = groups / numUniqueCombine inclusion–exclusion (join.cpp:1556-1568, utils.cpp:290-350) */
+typedef enum sge_tail_mode {
+    SGE_TAIL_SINGLE = 1,
+    SGE_TAIL_CHOOSE = 2,
+    SGE_TAIL_IEP = 3
+} sge_tail_mode;
+
+/* Join style.  WCOJ computes a level's candidates when the level is reached
+ * (generateCandidates, join.cpp:180-242); EXPLORATION intersects N(v) into the
+ * running candidate list of every later neighbour as soon as v is matched and
+ * prunes on an empty list (generateCandidates(DataGraph…), join.cpp:266-307;
+ * the reference's -i flag).  Counts are identical by construction. */
+typedef enum sge_join_style {
+    SGE_JOIN_WCOJ = 0,
+    SGE_JOIN_EXPLORATION = 1
+} sge_join_style;
+
+/* Root restriction between level 0 and level 1 (the two ends of the root edge). */
+typedef enum sge_root_kind {
+    SGE_ROOT_ANY = 0,      /* both orientations of every undirected edge */
+    SGE_ROOT_ASC = 1,      /* only m[0] < m[1] (getEdges(type), candidate_space.cpp:787-799) */
+    SGE_ROOT_DESC = 2      /* only m[0] > m[1] */
+} sge_root_kind;
+
+/*
+ * Plan blob: POD flattening of the facts the executor reads (the role of
+ * HyperTree + PrefixNode after refineIntersectionInfo, plan/decomposition.h:53-207).
+ * Levels are positions in the matching order; masks are over levels.
+ *
+ *   candidates(i) = ∩_{j ∈ parents[i]} N(m[j])
+ *                   ∩ { x : x > m[j] ∀ j ∈ lower[i] }        (largerAttrs, setBeginPos)
+ *                   ∩ { x : x < m[j] ∀ j ∈ upper[i] }        (smallerAttrs, setEndPos)
+ *                   \ { m[j] : j ∈ check[i] }                 (visited[] / checkExists)
+ *   base[i] (>=0): a level whose stored candidate list is a superset of level i's
+ *   list (candidatesBefore, plan/decomposition.h:32); rest[i] = the parents
+ *   still to intersect.  base[i] == -1: start from N(m[first_parent[i]]).
+ *
+ * Levels [0, num_enum) are enumerated; levels [num_enum, k) form the tail,
+ * counted by tail_mode.  For SGE_TAIL_IEP the count is
+ *   Σ_p coef[p] · Π_{b < nblocks[p]} S[block[p][b]]
+ * where S[mask] = |∩_{t ∈ mask} candidates(num_enum + t)|.
+ * The result per root is multiplied by count_multiplier (1, or |Aut| for
+ * single-bag plans: the reference counts embeddings there, instances elsewhere).
+ */
+typedef struct sge_plan_blob {
+    uint32_t magic;             /* SGE_PLAN_MAGIC */
+    uint32_t abi_version;       /* SGE_ABI_VERSION */
+    uint32_t k;                 /* pattern vertices, 3..SGE_MAX_K */
+    uint32_t num_enum;          /* enumerated levels, 2..k-1 */
+    uint32_t tail_mode;         /* sge_tail_mode */
+    uint32_t tail_len;          /* k - num_enum, 1..SGE_MAX_TAIL */
+    uint32_t join_style;        /* sge_join_style */
+    uint32_t root_kind;         /* sge_root_kind */
+    uint32_t order[SGE_MAX_K];  /* pattern vertex matched at level i */
+    uint32_t parents[SGE_MAX_K];
+    uint32_t lower[SGE_MAX_K];
+    uint32_t upper[SGE_MAX_K];
+    uint32_t check[SGE_MAX_K];
+    int32_t  base[SGE_MAX_K];
+    uint32_t rest[SGE_MAX_K];
+    uint32_t first_parent[SGE_MAX_K]; /* used when base[i] == -1 */
+    /* IEP partitions of the tail (only for SGE_TAIL_IEP) */
+    uint32_t num_partitions;
+    int32_t  part_coef[SGE_MAX_PARTITIONS];
+    uint32_t part_nblocks[SGE_MAX_PARTITIONS];
+    uint32_t part_block[SGE_MAX_PARTITIONS][SGE_MAX_TAIL]; /* masks over tail positions */
+    /* count semantics */
+    uint64_t count_multiplier;  /* 1 (instances) or |Aut| (single-bag: embeddings) */
+    uint64_t aut_size;          /* |Aut(pattern)| */
+    uint32_t single_bag;        /* 1 if the reference would run a one-bag plan */
+    uint32_t num_restrictions;  /* symmetry-breaking restrictions installed */
+    double   est_cost;          /* planner cost estimate (informational) */
+} sge_plan_blob;
+
+/* Planner options */
+typedef struct sge_plan_opts {
+    uint32_t join_style;        /* sge_join_style */
+    uint32_t use_iep;           /* 0: tails of length 1 only (no -u); 1: longest valid tail (-u) */
+    uint32_t max_tail;          /* cap on tail_len (<= SGE_MAX_TAIL) */
+    uint64_t seed;              /* seed for sampling-based cost estimates */
+    const uint32_t *force_order;/* optional: a full matching order to use (k entries) */
+} sge_plan_opts;
+
+/* Execution options */
+typedef struct sge_count_opts {
+    uint32_t blocks_per_sm;     /* 0 = occupancy-derived */
+    uint32_t warps_per_block;   /* 0 = default (8) */
+    uint32_t chunk;             /* root tasks per queue grab; 0 = auto */
+    double   time_budget_s;     /* 0 = unlimited; otherwise kernels stop and report SGE_TIMEOUT */
+    uint32_t max_level_capacity;/* 0 = graph max degree; smaller values exercise the overflow path */
+} sge_count_opts;
+
+/* Statistics of one sge_count call (per call, summed over plans) */
+typedef struct sge_stats {
+    double   kernel_ms;         /* device time of the counting kernels (CUDA events) */
+    double   total_ms;          /* host wall time of the call */
+    uint64_t root_tasks;        /* root edges processed */
+    uint64_t set_ops;           /* intersections/counting passes executed */
+    uint64_t alg_bytes;         /* algorithmic bytes: 4·(|A'|+|B'|) per set operation + 8 B per offset pair */
+    uint64_t partial_matches;   /* enumerated partial matches (all levels) */
+    uint32_t gpu_launches;      /* kernels launched by this call */
+    uint32_t status_flags;      /* bit0 overflow, bit1 timeout */
+} sge_stats;
+
+typedef struct sge_graph_info {
+    uint32_t num_vertices;
+    uint64_t num_directed_edges;  /* 2m */
+    uint32_t max_degree;
+    uint64_t device_bytes;        /* HBM held by the graph handle (CSR + root edges) */
+} sge_graph_info;
+
+typedef struct sge_graph sge_graph;
+typedef struct sge_plan sge_plan;
+
+/* ---- diagnostics ---- */
+/* sizeof of the ABI structs, for binding checks: 0 sge_plan_blob,
+ * 1 sge_plan_opts, 2 sge_count_opts, 3 sge_stats, 4 sge_graph_info,
+ * 5 sge_graph_stats. */
+size_t sge_struct_size(int which);
+const char *sge_last_error(void);
+const char *sge_version(void);
+int sge_device_count(void);
+
+/* ---- host-side graph I/O (replaces DataGraph::loadDataGraph / loadBinaryGraph,
+ *      relation/graph.cpp:255-419, and PatternGraph::loadPatternGraph, :661-770) ----
+ * Results are malloc'ed; release them with sge_free_host. */
+sge_status sge_load_graph_file(const char *path, uint32_t **offsets, uint32_t **nbrs,
+                               uint32_t *num_vertices, uint64_t *num_directed_edges);
+sge_status sge_save_graph_binary(const char *path, const uint32_t *offsets, const uint32_t *nbrs,
+                                 uint32_t num_vertices);
+sge_status sge_load_pattern_file(const char *path, uint32_t *k, uint32_t *m, uint32_t *edges /* 2*m, cap 2*SGE_MAX_K*SGE_MAX_K */);
+/* CSR from an undirected edge list (u,v pairs): symmetric, per-list sorted
+ * (Graph::addDirectedEdges, graph.cpp:143-173).  dedup!=0 also removes
+ * duplicates and self-loops (the reference does not; its inputs must be clean). */
+sge_status sge_csr_from_edges(const uint32_t *edges, uint64_t m, uint32_t num_vertices, int dedup,
+                              uint32_t **offsets, uint32_t **nbrs, uint64_t *num_directed_edges);
+void sge_free_host(void *p);
+
+/* ---- seeded synthetic generators (deterministic on every host) ---- */
+/* R-MAT: 2^scale vertices, m undirected edge draws; a,b,c in units of 1e-6 (d = rest).
+ * Output: deduplicated, self-loop-free undirected edges with u<v, sorted. */
+sge_status sge_gen_rmat(uint32_t scale, uint64_t m, uint32_t a_ppm, uint32_t b_ppm, uint32_t c_ppm,
+                        uint64_t seed, uint32_t **edges, uint64_t *m_out);
+/* Chung-Lu: expected degrees ∝ (i+1)^(-1/(gamma-1)), mean 2m/n, capped at
+ * max_deg (0 = n-1); m distinct undirected edges, u<v, sorted. */
+sge_status sge_gen_chung_lu(uint32_t n, uint64_t m, uint32_t gamma_milli, uint32_t max_deg, uint64_t seed,
+                            uint32_t **edges, uint64_t *m_out);
+/* Random connected pattern with k vertices and m edges (k-1 <= m <= k(k-1)/2). */
+sge_status sge_gen_pattern(uint32_t k, uint32_t m, uint64_t seed, uint32_t *edges /* 2*m */);
+
+/* Degree/clustering statistics the planner's cost model reads (host only). */
+typedef struct sge_graph_stats {
+    double num_vertices;
+    double num_directed_edges;
+    double moments[SGE_MAX_K + 2];  /* M_j = Σ_v deg(v)^j */
+    double clustering;              /* sampled global clustering coefficient */
+    double max_degree;
+} sge_graph_stats;
+sge_status sge_graph_stats_compute(const uint32_t *offsets, const uint32_t *nbrs, uint32_t num_vertices,
+                                   sge_graph_stats *out);
+
+/* ---- planner (host; stands in for optCostPlan + selectSymmetry +
+ *      buildTraverseUnlabeled + refineIntersectionInfo, main.cpp:60-69) ---- */
+sge_status sge_plan_pattern(uint32_t k, uint32_t m, const uint32_t *edges,
+                            const sge_graph *g /* may be NULL: degree stats unknown */,
+                            const sge_plan_opts *opts, sge_plan_blob *out);
+/* Same, from precomputed statistics (no device needed). */
+sge_status sge_plan_pattern_stats(uint32_t k, uint32_t m, const uint32_t *edges, const sge_graph_stats *stats,
+                                  const sge_plan_opts *opts, sge_plan_blob *out);
+/* |Aut(P)| and whether the reference would run a single-bag plan. */
+sge_status sge_pattern_info(uint32_t k, uint32_t m, const uint32_t *edges,
+                            uint64_t *aut_size, uint32_t *single_bag);
+/* Check a plan blob for internal consistency (levels, masks, tail validity). */
+sge_status sge_plan_validate(const sge_plan_blob *blob);
+
+/* ---- device graph (replaces the DataGraph/CandidateSpace the join reads) ---- */
+sge_status sge_graph_create(const uint32_t *offsets, const uint32_t *nbrs, uint32_t num_vertices,
+                            uint64_t num_directed_edges, int device, sge_graph **out);
+sge_status sge_graph_destroy(sge_graph *g);
+sge_status sge_graph_get_info(const sge_graph *g, sge_graph_info *info);
+
+/* ---- compiled plans ---- */
+sge_status sge_plan_create(const sge_plan_blob *blob, sge_plan **out);
+sge_status sge_plan_destroy(sge_plan *p);
+
+/* ---- execution (replaces sharedJoin / parSharedJoin) ----
+ * Counts nplans patterns over g in one persistent launch (the batch shares
+ * the graph and a global work queue).  counts[i] receives the reference's
+ * "Number of matches" for plan i; instances[i] (may be NULL) the count of
+ * subgraph instances (embeddings / |Aut|). */
+sge_status sge_count(sge_graph *g, const sge_plan *const *plans, uint32_t nplans,
+                     const sge_count_opts *opts, uint64_t *counts, uint64_t *instances,
+                     sge_stats *stats);
+/* End-to-end convenience: host CSR in, counts out (H2D copy, count, D2H read
+ * and release all inside the call). */
+sge_status sge_count_host(const uint32_t *offsets, const uint32_t *nbrs, uint32_t num_vertices,
+                          uint64_t num_directed_edges, const sge_plan_blob *blobs, uint32_t nplans,
+                          const sge_count_opts *opts, uint64_t *counts, sge_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SGE_H */

@@ -1,0 +1,122 @@
+"""ctypes binding of liboracle.so (oracle/sge_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline/reference arm, never by the product.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+SO = Path(__file__).resolve().parent / "_build" / "liboracle.so"
+_lib = None
+u32, u64 = C.c_uint32, C.c_uint64
+_P = C.POINTER
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not SO.exists():
+            raise FileNotFoundError(f"{SO} missing: run __graft_entry__.build()")
+        L = C.CDLL(str(SO))
+        L.oracle_choosec_ref.restype = u64
+        L.oracle_choosec_ref.argtypes = [u64, C.c_int]
+        L.oracle_binom_exact.restype = u64
+        L.oracle_binom_exact.argtypes = [u64, C.c_int]
+        L.oracle_set_begin_pos.restype = u32
+        L.oracle_set_begin_pos.argtypes = [_P(u32), u32, u32]
+        L.oracle_set_end_pos.restype = u32
+        L.oracle_set_end_pos.argtypes = [_P(u32), u32, u32]
+        L.oracle_intersect.restype = u32
+        L.oracle_intersect.argtypes = [_P(u32), u32, _P(u32), u32, _P(u32)]
+        L.oracle_intersect_count.restype = u32
+        L.oracle_intersect_count.argtypes = [_P(u32), u32, _P(u32), u32]
+        L.oracle_num_results.restype = u64
+        L.oracle_num_results.argtypes = [_P(u32), u32, _P(u32), _P(u32), u32, _P(u32), u32, _P(u32), u32]
+        L.oracle_num_unique_combine.restype = u64
+        L.oracle_num_unique_combine.argtypes = [_P(_P(u32)), _P(u32), C.c_int]
+        L.oracle_aut_size.restype = u64
+        L.oracle_aut_size.argtypes = [u32, u32, _P(u32)]
+        L.oracle_bruteforce_embeddings.restype = u64
+        L.oracle_bruteforce_embeddings.argtypes = [_P(u32), _P(u32), u32, u32, u32, _P(u32), C.c_int]
+        L.oracle_count_plan.restype = u64
+        L.oracle_count_plan.argtypes = [_P(u32), _P(u32), u32, C.c_void_p, C.c_int, u64, u64, _P(u64)]
+        L.oracle_max_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(_P(u32))
+
+
+def _arr(x) -> np.ndarray:
+    return np.ascontiguousarray(x, dtype=np.uint32)
+
+
+def choosec_ref(n: int, k: int) -> int:
+    return int(lib().oracle_choosec_ref(n, k))
+
+
+def binom_exact(n: int, k: int) -> int:
+    return int(lib().oracle_binom_exact(n, k))
+
+
+def set_begin_pos(a, bound: int) -> int:
+    a = _arr(a)
+    return int(lib().oracle_set_begin_pos(_p(a), a.size, bound))
+
+
+def set_end_pos(a, bound: int) -> int:
+    a = _arr(a)
+    return int(lib().oracle_set_end_pos(_p(a), a.size, bound))
+
+
+def intersect(a, b) -> np.ndarray:
+    a, b = _arr(a), _arr(b)
+    out = np.zeros(max(min(a.size, b.size), 1), np.uint32)
+    n = lib().oracle_intersect(_p(a), a.size, _p(b), b.size, _p(out))
+    return out[:n]
+
+
+def intersect_count(a, b) -> int:
+    a, b = _arr(a), _arr(b)
+    return int(lib().oracle_intersect_count(_p(a), a.size, _p(b), b.size))
+
+
+def num_results(values, part_match, to_check, larger, smaller) -> int:
+    v, pm, tc, lg, sm = map(_arr, (values, part_match, to_check, larger, smaller))
+    return int(lib().oracle_num_results(_p(v), v.size, _p(pm), _p(tc), tc.size, _p(lg), lg.size, _p(sm), sm.size))
+
+
+def num_unique_combine(sets) -> int:
+    arrs = [_arr(s) for s in sets]
+    ptrs = (_P(u32) * len(arrs))(*[_p(a) for a in arrs])
+    lens = (u32 * len(arrs))(*[a.size for a in arrs])
+    return int(lib().oracle_num_unique_combine(ptrs, lens, len(arrs)))
+
+
+def aut_size(k: int, edges) -> int:
+    e = _arr(edges).reshape(-1)
+    return int(lib().oracle_aut_size(k, e.size // 2, _p(e)))
+
+
+def bruteforce_embeddings(offsets, nbrs, k: int, edges, threads: int = 0) -> int:
+    off, nb, e = _arr(offsets), _arr(nbrs), _arr(edges).reshape(-1)
+    return int(lib().oracle_bruteforce_embeddings(_p(off), _p(nb), off.size - 1, k, e.size // 2, _p(e), threads))
+
+
+def count_plan(offsets, nbrs, blob, threads: int = 0, stride: int = 1, offset: int = 0) -> tuple[int, int]:
+    """Runs a plan blob on the CPU.  Returns (instances over the sampled roots, roots done)."""
+    off, nb = _arr(offsets), _arr(nbrs)
+    done = u64()
+    r = lib().oracle_count_plan(_p(off), _p(nb), off.size - 1, C.addressof(blob), threads, stride, offset,
+                                C.byref(done))
+    return int(r), int(done.value)
+
+
+def max_threads() -> int:
+    return int(lib().oracle_max_threads())

@@ -1,0 +1,457 @@
+/*
+ * sge_oracle.c — CPU oracle for the subgraph-enumeration hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the product links or calls this file:
+ * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference
+ * arm load liboracle.so, as the checker or as the timed CPU baseline.
+ *
+ * It holds three things:
+ *  1. plain-C restatements of the reference's hot-path primitives, each citing
+ *     the function it follows (paths relative to the reference project root);
+ *  2. an independent brute-force counter (embeddings, |Aut|, instances) used to
+ *     pin count semantics (instances for multi-bag plans, embeddings for
+ *     single-bag plans);
+ *  3. a CPU executor for sge_plan_blob built from the primitives in (1),
+ *     following the reference's join structure (generateCandidates →
+ *     MultiIntersection → DFS; traverse → numResults / choosec /
+ *     numUniqueCombine at the leaf), parallel over root edges with OpenMP like
+ *     parSharedJoin (matching/parallel.cpp:1154-1486).
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../include/sge.h"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define BST 32 /* BINARY_SEARCH_THRESHOLD, config/config.h:37 */
+
+/* ---------------------------------------------------------------- 1 ---- */
+
+/* choosec — utility/utils.cpp:80-94.  nom = n(n-1)…(n-k+1) accumulated in
+ * uint64 (wrapping), denom = k!, result nom/denom.  Kept with the wrap so
+ * tests can show where it departs from the exact binomial. */
+uint64_t oracle_choosec_ref(uint64_t n, int k) {
+    if ((uint64_t)k > n) return 0;
+    if (k == 0) return 1;
+    uint64_t nom = n, denom = 1;
+    for (int i = 1; i < k; i++) {
+        nom *= (n - (uint64_t)i);
+        denom *= (uint64_t)(i + 1);
+    }
+    return nom / denom;
+}
+
+/* Exact C(n,k) mod 2^64 via 128-bit intermediates (what the executors use). */
+uint64_t oracle_binom_exact(uint64_t n, int k) {
+    if ((uint64_t)k > n) return 0;
+    unsigned __int128 acc = 1;
+    for (int i = 0; i < k; i++) acc = acc * (unsigned __int128)(n - (uint64_t)i) / (unsigned __int128)(i + 1);
+    return (uint64_t)acc;
+}
+
+/* setBeginPos — utility/utils.cpp:581-597: first position with a[j] > maxCompared
+ * (linear scan up to BINARY_SEARCH_THRESHOLD, else upper_bound). */
+uint32_t oracle_set_begin_pos(const uint32_t *a, uint32_t count, uint32_t maxCompared) {
+    uint32_t beginPos = 0;
+    if (count <= BST) {
+        for (uint32_t j = 0; j < count; ++j)
+            if (a[j] > maxCompared) { beginPos = j; break; }
+        if (beginPos == 0 && count > 0 && a[count - 1] <= maxCompared) beginPos = count;
+    } else {
+        uint32_t lo = 0, n = count;
+        while (n > 0) {
+            uint32_t h = n >> 1;
+            if (a[lo + h] <= maxCompared) { lo += h + 1; n -= h + 1; } else n = h;
+        }
+        beginPos = lo;
+    }
+    return beginPos;
+}
+
+/* setEndPos — utility/utils.cpp:599-612: first position with a[j] >= minCompared. */
+uint32_t oracle_set_end_pos(const uint32_t *a, uint32_t count, uint32_t minCompared) {
+    uint32_t endPos = count;
+    if (count <= BST) {
+        for (uint32_t j = 0; j < count; ++j)
+            if (a[j] >= minCompared) { endPos = j; break; }
+    } else {
+        uint32_t lo = 0, n = count;
+        while (n > 0) {
+            uint32_t h = n >> 1;
+            if (a[lo + h] < minCompared) { lo += h + 1; n -= h + 1; } else n = h;
+        }
+        endPos = lo;
+    }
+    return endPos;
+}
+
+/* GallopingSearch — utility/compute_set_intersection.cpp:89-119: first index
+ * in [begin, end) with src[i] >= val, by doubling steps then binary search. */
+static uint32_t galloping_search(const uint32_t *src, uint32_t begin, uint32_t end, uint32_t target) {
+    if (begin >= end || src[end - 1] < target) return end;
+    if (src[begin] >= target) return begin;
+    uint32_t offset = 1;
+    while (begin + offset < end && src[begin + offset] < target) offset <<= 1;
+    uint32_t lo = begin + (offset >> 1), hi = (begin + offset < end) ? begin + offset : end;
+    while (lo < hi) {
+        uint32_t mid = lo + ((hi - lo) >> 1);
+        if (src[mid] < target) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+/* ComputeCandidates (output) — utility/compute_set_intersection.cpp:10-45 with
+ * the scalar kernels of :1136-1327: galloping when one list is more than 50×
+ * the other, merge otherwise.  out may alias a. */
+uint32_t oracle_intersect(const uint32_t *a, uint32_t na, const uint32_t *b, uint32_t nb, uint32_t *out) {
+    uint32_t cnt = 0;
+    if (na == 0 || nb == 0) return 0;
+    if (na / nb > 50 || nb / na > 50) {
+        const uint32_t *s = na < nb ? a : b, *l = na < nb ? b : a;
+        uint32_t ns = na < nb ? na : nb, nl = na < nb ? nb : na;
+        uint32_t li = 0;
+        for (uint32_t si = 0; si < ns; ++si) {
+            li = galloping_search(l, li, nl, s[si]);
+            if (li >= nl) break;
+            if (l[li] == s[si]) { out[cnt++] = s[si]; ++li; }
+        }
+        return cnt;
+    }
+    uint32_t i = 0, j = 0;
+    while (i < na && j < nb) {
+        if (a[i] < b[j]) ++i;
+        else if (a[i] > b[j]) ++j;
+        else { out[cnt++] = a[i]; ++i; ++j; }
+    }
+    return cnt;
+}
+
+/* ComputeCandidates (count only) — compute_set_intersection.cpp:47-87: the
+ * galloping switch happens above a 32× ratio. */
+uint32_t oracle_intersect_count(const uint32_t *a, uint32_t na, const uint32_t *b, uint32_t nb) {
+    uint32_t cnt = 0;
+    if (na == 0 || nb == 0) return 0;
+    if (na / nb > 32 || nb / na > 32) {
+        const uint32_t *s = na < nb ? a : b, *l = na < nb ? b : a;
+        uint32_t ns = na < nb ? na : nb, nl = na < nb ? nb : na;
+        uint32_t li = 0;
+        for (uint32_t si = 0; si < ns; ++si) {
+            li = galloping_search(l, li, nl, s[si]);
+            if (li >= nl) break;
+            if (l[li] == s[si]) { ++cnt; ++li; }
+        }
+        return cnt;
+    }
+    uint32_t i = 0, j = 0;
+    while (i < na && j < nb) {
+        if (a[i] < b[j]) ++i;
+        else if (a[i] > b[j]) ++j;
+        else { ++cnt; ++i; ++j; }
+    }
+    return cnt;
+}
+
+/* checkExists — relation/relation.cpp:206-232: position of target in
+ * [begin, end) or end. */
+static uint32_t check_exists(const uint32_t *a, uint32_t begin, uint32_t end, uint32_t target) {
+    uint32_t lo = begin, hi = end;
+    while (lo < hi) {
+        uint32_t mid = lo + ((hi - lo) >> 1);
+        if (a[mid] < target) lo = mid + 1; else hi = mid;
+    }
+    return (lo < end && a[lo] == target) ? lo : end;
+}
+
+/* TrieLevel::numResults — relation/relation.cpp:301-338: range after the
+ * larger/smaller bounds, minus every already-matched vertex found inside it. */
+uint64_t oracle_num_results(const uint32_t *values, uint32_t length, const uint32_t *partMatch,
+                            const uint32_t *toCheck, uint32_t nCheck, const uint32_t *larger, uint32_t nLarger,
+                            const uint32_t *smaller, uint32_t nSmaller) {
+    uint32_t maxCompared = 0, minCompared = 0xFFFFFFFFu;
+    for (uint32_t i = 0; i < nLarger; ++i) if (partMatch[larger[i]] > maxCompared) maxCompared = partMatch[larger[i]];
+    for (uint32_t i = 0; i < nSmaller; ++i) if (partMatch[smaller[i]] < minCompared) minCompared = partMatch[smaller[i]];
+    uint32_t beginPos = 0, endPos = length;
+    if (nLarger) beginPos = oracle_set_begin_pos(values, length, maxCompared);
+    if (nSmaller) endPos = oracle_set_end_pos(values, length, minCompared);
+    if (endPos < beginPos) endPos = beginPos;
+    uint64_t num = endPos - beginPos;
+    for (uint32_t i = 0; i < nCheck; ++i)
+        if (check_exists(values, beginPos, endPos, partMatch[toCheck[i]]) != endPos) --num;
+    return num;
+}
+
+/* numUniqueCombine — utility/utils.cpp:290-350: number of tuples with one
+ * element from each set and all elements distinct, by inclusion–exclusion over
+ * subsets of the pairwise "equal" events; each chosen pair set is reduced with
+ * a union-find and contributes Π |∩ sets of a component|.  Sets are sorted. */
+static uint32_t uf_find(uint32_t *p, uint32_t x) { while (p[x] != x) x = p[x] = p[p[x]]; return x; }
+uint64_t oracle_num_unique_combine(const uint32_t *const *sets, const uint32_t *lens, int nsets) {
+    if (nsets <= 0) return 1;
+    if (nsets > 6) return 0; /* 15 pairs → 2^15 subsets: enough for the tails here */
+    uint64_t num = 1;
+    for (int i = 0; i < nsets; ++i) num *= lens[i];
+    int np = 0, pa[15], pb[15];
+    for (int i = 0; i < nsets; ++i)
+        for (int j = i + 1; j < nsets; ++j) { pa[np] = i; pb[np] = j; ++np; }
+    uint32_t maxlen = 0;
+    for (int i = 0; i < nsets; ++i) if (lens[i] > maxlen) maxlen = lens[i];
+    uint32_t *tmp = (uint32_t *)malloc(sizeof(uint32_t) * (maxlen + 1));
+    uint32_t *tmp2 = (uint32_t *)malloc(sizeof(uint32_t) * (maxlen + 1));
+    for (uint32_t choice = 1; choice < (1u << np); ++choice) {
+        uint32_t par[8];
+        for (int i = 0; i < nsets; ++i) par[i] = (uint32_t)i;
+        for (int q = 0; q < np; ++q)
+            if ((choice >> q) & 1u) {
+                uint32_t x = uf_find(par, (uint32_t)pa[q]), y = uf_find(par, (uint32_t)pb[q]);
+                if (x != y) par[x] = y;
+            }
+        uint64_t term = 1;
+        for (int r = 0; r < nsets; ++r) {
+            if (uf_find(par, (uint32_t)r) != (uint32_t)r) continue;
+            /* component rooted at r: intersect its sets */
+            int first = 1;
+            uint32_t n = 0;
+            for (int i = 0; i < nsets; ++i) {
+                if (uf_find(par, (uint32_t)i) != (uint32_t)r) continue;
+                if (first) { memcpy(tmp, sets[i], sizeof(uint32_t) * lens[i]); n = lens[i]; first = 0; }
+                else { n = oracle_intersect(tmp, n, sets[i], lens[i], tmp2); memcpy(tmp, tmp2, sizeof(uint32_t) * n); }
+            }
+            term *= n;
+        }
+        if (__builtin_popcount(choice) % 2 == 0) num += term; else num -= term;
+    }
+    free(tmp);
+    free(tmp2);
+    return num;
+}
+
+/* ---------------------------------------------------------------- 2 ---- */
+
+static int pat_edge(const uint32_t *adj, uint32_t a, uint32_t b) { return (adj[a] >> b) & 1u; }
+
+/* |Aut(P)| by enumerating adjacency-preserving permutations (k <= 10). */
+uint64_t oracle_aut_size(uint32_t k, uint32_t m, const uint32_t *edges) {
+    uint32_t adj[32] = {0};
+    for (uint32_t i = 0; i < m; ++i) { adj[edges[2 * i]] |= 1u << edges[2 * i + 1]; adj[edges[2 * i + 1]] |= 1u << edges[2 * i]; }
+    uint32_t map[32], used = 0, next[33];
+    uint64_t cnt = 0;
+    int i = 0;
+    next[0] = 0;
+    while (i >= 0) {
+        if (i == (int)k) { ++cnt; --i; if (i >= 0) used &= ~(1u << map[i]); continue; }
+        int placed = 0;
+        for (uint32_t c = next[i]; c < k; ++c) {
+            if ((used >> c) & 1u) continue;
+            int ok = 1;
+            for (int j = 0; j < i && ok; ++j) if (pat_edge(adj, (uint32_t)i, (uint32_t)j) != pat_edge(adj, c, map[j])) ok = 0;
+            if (!ok) continue;
+            map[i] = c; used |= 1u << c; next[i] = c + 1; ++i; if (i < (int)k) next[i] = 0; placed = 1; break;
+        }
+        if (!placed) { --i; if (i >= 0) used &= ~(1u << map[i]); }
+    }
+    return cnt;
+}
+
+static int has_edge(const uint32_t *off, const uint32_t *nb, uint32_t u, uint32_t v) {
+    uint32_t a = off[u], b = off[u + 1];
+    return check_exists(nb, a, b, v) != b;
+}
+
+/* Injective homomorphisms (embeddings) of a connected pattern, by DFS over a
+ * connected order; each new vertex ranges over the neighbours of its first
+ * earlier neighbour and is checked against all other earlier neighbours. */
+uint64_t oracle_bruteforce_embeddings(const uint32_t *off, const uint32_t *nb, uint32_t n, uint32_t k, uint32_t m,
+                                      const uint32_t *edges, int threads) {
+    uint32_t adj[32] = {0};
+    for (uint32_t i = 0; i < m; ++i) { adj[edges[2 * i]] |= 1u << edges[2 * i + 1]; adj[edges[2 * i + 1]] |= 1u << edges[2 * i]; }
+    uint32_t order[32], pos[32], seen = 0;
+    /* start at the max-degree vertex, then greedily most-connected */
+    uint32_t best = 0;
+    for (uint32_t u = 1; u < k; ++u) if (__builtin_popcount(adj[u]) > __builtin_popcount(adj[best])) best = u;
+    order[0] = best; seen = 1u << best;
+    for (uint32_t i = 1; i < k; ++i) {
+        int bv = -1, bs = -1;
+        for (uint32_t u = 0; u < k; ++u) {
+            if ((seen >> u) & 1u) continue;
+            int s = __builtin_popcount(adj[u] & seen);
+            if (s > 0 && s > bs) { bs = s; bv = (int)u; }
+        }
+        if (bv < 0) return 0; /* disconnected */
+        order[i] = (uint32_t)bv; seen |= 1u << bv;
+    }
+    for (uint32_t i = 0; i < k; ++i) pos[order[i]] = i;
+    uint32_t back[32], first[32];
+    for (uint32_t i = 0; i < k; ++i) {
+        back[i] = 0;
+        for (uint32_t j = 0; j < i; ++j) if (pat_edge(adj, order[i], order[j])) back[i] |= 1u << j;
+        first[i] = back[i] ? (uint32_t)__builtin_ctz(back[i]) : 0;
+    }
+    (void)pos;
+    uint64_t total = 0;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : total)
+#endif
+    for (int64_t r = 0; r < (int64_t)n; ++r) {
+        uint32_t mm[32], it[32];
+        int lv = 0;
+        mm[0] = (uint32_t)r;
+        if (k == 1) { total += 1; continue; }
+        lv = 1;
+        it[1] = off[mm[first[1]]];
+        while (lv >= 1) {
+            uint32_t p = mm[first[lv]];
+            if (it[lv] >= off[p + 1]) { --lv; continue; }
+            uint32_t x = nb[it[lv]++];
+            int ok = 1;
+            for (int j = 0; j < lv && ok; ++j) if (mm[j] == x) ok = 0;
+            for (uint32_t msk = back[lv] & ~(1u << first[lv]); msk && ok; msk &= msk - 1)
+                if (!has_edge(off, nb, mm[__builtin_ctz(msk)], x)) ok = 0;
+            if (!ok) continue;
+            mm[lv] = x;
+            if (lv + 1 == (int)k) { total += 1; continue; }
+            ++lv;
+            it[lv] = off[mm[first[lv]]];
+        }
+    }
+    return total;
+}
+
+/* ---------------------------------------------------------------- 3 ---- */
+
+typedef struct {
+    const uint32_t *off, *nb;
+    const sge_plan_blob *p;
+    uint32_t maxdeg;
+} exec_ctx;
+
+/* Candidates of level i: bound-trim every parent list (setBeginPos /
+ * setEndPos as in generateCandidates, matching/join.cpp:137-178), intersect
+ * them pairwise shortest-first (MultiIntersection, compute_set_intersection.cpp:308-342),
+ * then drop the matched vertices of check[i] (visited[]). */
+static uint32_t level_candidates(const exec_ctx *c, uint32_t i, const uint32_t *mm, uint32_t *out, uint32_t *tmp) {
+    const sge_plan_blob *p = c->p;
+    uint32_t lo = 0, hi = 0xFFFFFFFFu;
+    int has_lo = p->lower[i] != 0, has_hi = p->upper[i] != 0;
+    for (uint32_t msk = p->lower[i]; msk; msk &= msk - 1) if (mm[__builtin_ctz(msk)] > lo) lo = mm[__builtin_ctz(msk)];
+    for (uint32_t msk = p->upper[i]; msk; msk &= msk - 1) if (mm[__builtin_ctz(msk)] < hi) hi = mm[__builtin_ctz(msk)];
+    const uint32_t *lists[32];
+    uint32_t lens[32], nl = 0;
+    for (uint32_t msk = p->parents[i]; msk; msk &= msk - 1) {
+        uint32_t v = mm[__builtin_ctz(msk)];
+        const uint32_t *a = c->nb + c->off[v];
+        uint32_t len = c->off[v + 1] - c->off[v];
+        if (has_lo) { uint32_t b = oracle_set_begin_pos(a, len, lo); a += b; len -= b; }
+        if (has_hi) len = oracle_set_end_pos(a, len, hi);
+        lists[nl] = a; lens[nl] = len; ++nl;
+    }
+    /* shortest first */
+    for (uint32_t x = 0; x < nl; ++x)
+        for (uint32_t y = x + 1; y < nl; ++y)
+            if (lens[y] < lens[x]) {
+                const uint32_t *t = lists[x]; lists[x] = lists[y]; lists[y] = t;
+                uint32_t tl = lens[x]; lens[x] = lens[y]; lens[y] = tl;
+            }
+    uint32_t n = lens[0];
+    memcpy(out, lists[0], sizeof(uint32_t) * n);
+    for (uint32_t l = 1; l < nl && n; ++l) {
+        n = oracle_intersect(out, n, lists[l], lens[l], tmp);
+        memcpy(out, tmp, sizeof(uint32_t) * n);
+    }
+    uint32_t w = 0;
+    for (uint32_t e = 0; e < n; ++e) {
+        int ex = 0;
+        for (uint32_t msk = p->check[i]; msk; msk &= msk - 1) if (mm[__builtin_ctz(msk)] == out[e]) ex = 1;
+        if (!ex) out[w++] = out[e];
+    }
+    return w;
+}
+
+/* Leaf count (traverse, matching/join.cpp:1520-1691). */
+static uint64_t tail_count(const exec_ctx *c, const uint32_t *mm, uint32_t **bufs, uint32_t *tmp) {
+    const sge_plan_blob *p = c->p;
+    const uint32_t ne = p->num_enum, T = p->tail_len;
+    if (p->tail_mode == SGE_TAIL_SINGLE || p->tail_mode == SGE_TAIL_CHOOSE) {
+        uint32_t n = level_candidates(c, ne, mm, bufs[0], tmp);
+        return p->tail_mode == SGE_TAIL_SINGLE ? (uint64_t)n : oracle_binom_exact(n, (int)T);
+    }
+    const uint32_t *sets[SGE_MAX_TAIL];
+    uint32_t lens[SGE_MAX_TAIL];
+    for (uint32_t t = 0; t < T; ++t) {
+        lens[t] = level_candidates(c, ne + t, mm, bufs[t], tmp);
+        sets[t] = bufs[t];
+    }
+    return oracle_num_unique_combine(sets, lens, (int)T);
+}
+
+/* Runs the plan over root tasks t ≡ offset (mod stride).  Returns the sum of
+ * per-root counts (instances; multiply by count_multiplier for the
+ * reference's number). */
+uint64_t oracle_count_plan(const uint32_t *off, const uint32_t *nb, uint32_t n, const sge_plan_blob *p, int threads,
+                           uint64_t stride, uint64_t offset, uint64_t *roots_done) {
+    exec_ctx c;
+    c.off = off; c.nb = nb; c.p = p; c.maxdeg = 0;
+    for (uint32_t v = 0; v < n; ++v) if (off[v + 1] - off[v] > c.maxdeg) c.maxdeg = off[v + 1] - off[v];
+    /* root edge list u<v */
+    uint64_t m = off[n] / 2, w = 0;
+    uint32_t *eu = (uint32_t *)malloc(sizeof(uint32_t) * (m + 1)), *ev = (uint32_t *)malloc(sizeof(uint32_t) * (m + 1));
+    for (uint32_t u = 0; u < n; ++u)
+        for (uint32_t e = off[u]; e < off[u + 1]; ++e)
+            if (nb[e] > u) { eu[w] = u; ev[w] = nb[e]; ++w; }
+    const uint64_t ntasks = (p->root_kind == SGE_ROOT_ANY) ? 2 * m : m;
+    if (stride == 0) stride = 1;
+    uint64_t total = 0, done = 0;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel reduction(+ : total, done)
+#endif
+    {
+        const uint32_t K = p->k, ne = p->num_enum;
+        uint32_t *bufs[SGE_MAX_K + SGE_MAX_TAIL];
+        for (uint32_t i = 0; i < SGE_MAX_K + SGE_MAX_TAIL; ++i) bufs[i] = (uint32_t *)malloc(sizeof(uint32_t) * (c.maxdeg + 1));
+        uint32_t *tmp = (uint32_t *)malloc(sizeof(uint32_t) * (c.maxdeg + 1));
+        uint32_t cnt[SGE_MAX_K], it[SGE_MAX_K], mm[SGE_MAX_K];
+        (void)K;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 64)
+#endif
+        for (int64_t ti = (int64_t)offset; ti < (int64_t)ntasks; ti += (int64_t)stride) {
+            uint64_t t = (uint64_t)ti;
+            uint32_t a, b;
+            if (p->root_kind == SGE_ROOT_ANY) { a = eu[t >> 1]; b = ev[t >> 1]; if (t & 1) { uint32_t x = a; a = b; b = x; } }
+            else { a = eu[t]; b = ev[t]; if (p->root_kind == SGE_ROOT_DESC) { uint32_t x = a; a = b; b = x; } }
+            mm[0] = a; mm[1] = b;
+            ++done;
+            if (ne == 2) { total += tail_count(&c, mm, bufs + SGE_MAX_K, tmp); continue; }
+            int lv = 2;
+            cnt[2] = level_candidates(&c, 2, mm, bufs[2], tmp);
+            it[2] = 0;
+            while (lv >= 2) {
+                if (it[lv] >= cnt[lv]) { --lv; continue; }
+                mm[lv] = bufs[lv][it[lv]++];
+                if ((uint32_t)lv + 1 == ne) { total += tail_count(&c, mm, bufs + SGE_MAX_K, tmp); continue; }
+                ++lv;
+                cnt[lv] = level_candidates(&c, (uint32_t)lv, mm, bufs[lv], tmp);
+                it[lv] = 0;
+            }
+        }
+        for (uint32_t i = 0; i < SGE_MAX_K + SGE_MAX_TAIL; ++i) free(bufs[i]);
+        free(tmp);
+    }
+    free(eu);
+    free(ev);
+    if (roots_done) *roots_done = done;
+    return total;
+}
+
+int oracle_max_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

@@ -1,0 +1,156 @@
+// graph_mining_system — drop-in for the reference's binary of the same name
+// (main.cpp:12-230, utility/command.cpp:8-56).  Same flags and log keys:
+//   -q query  -d data  [-r result-log]  [-i] (exploration-style)  [-u] (IEP)
+//   [-t threads]  [--help|-h]
+// plus additive flags: --device N, --batch LIST (one pattern path per line,
+// counted in one persistent launch), --seed S.
+// Like the reference, -r redirects the text log to a file.  Planning runs on
+// the host; the join runs on the GPU through libsge.
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <string>
+#include <vector>
+
+#include "sge.h"
+
+namespace {
+
+struct Args {
+    std::string q, d, r, batch;
+    bool iep = false, explore = false, help = false;
+    int threads = 0, device = 0;
+    unsigned long long seed = 1;
+};
+
+bool parse(int argc, char **argv, Args &a) {
+    for (int i = 1; i < argc; ++i) {
+        std::string s = argv[i];
+        auto need = [&](std::string &dst) {
+            if (i + 1 >= argc) return false;
+            dst = argv[++i];
+            return true;
+        };
+        std::string v;
+        if (s == "-q") { if (!need(a.q)) return false; }
+        else if (s == "-d") { if (!need(a.d)) return false; }
+        else if (s == "-r") { if (!need(a.r)) return false; }
+        else if (s == "-i") a.explore = true;
+        else if (s == "-u") a.iep = true;
+        else if (s == "-t") { if (!need(v)) return false; a.threads = atoi(v.c_str()); }
+        else if (s == "--device") { if (!need(v)) return false; a.device = atoi(v.c_str()); }
+        else if (s == "--batch") { if (!need(a.batch)) return false; }
+        else if (s == "--seed") { if (!need(v)) return false; a.seed = strtoull(v.c_str(), nullptr, 10); }
+        else if (s == "-h" || s == "--help") a.help = true;
+        else { std::cerr << "unknown option " << s << "\n"; return false; }
+    }
+    return true;
+}
+
+void usage() {
+    std::cout << "Usage: graph_mining_system -q QUERY -d DATA [-r RESULT] [-i] [-u] [-t THREADS]\n"
+                 "       [--device N] [--batch PATTERN_LIST] [--seed S]\n"
+                 "  -q  query graph path\n  -d  data graph path (text or BINGRPH)\n"
+                 "  -r  result path (log destination)\n  -i  exploration-style intersection\n"
+                 "  -u  IEP counting of the last levels\n  -t  threads (accepted; the GPU uses all SMs)\n";
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+    Args a;
+    if (!parse(argc, argv, a) || a.help || (a.q.empty() && a.batch.empty()) || a.d.empty()) {
+        usage();
+        return a.help ? 0 : 1;
+    }
+    std::ofstream file;
+    if (!a.r.empty()) file.open(a.r);
+    std::ostream &out = a.r.empty() ? std::cout : file;
+    std::vector<std::string> queries;
+    if (!a.batch.empty()) {
+        std::ifstream bl(a.batch);
+        if (!bl) { std::cout << "Can not open file " << a.batch << "!" << std::endl; return 1; }
+        std::string line;
+        while (std::getline(bl, line)) if (!line.empty()) queries.push_back(line);
+    } else {
+        queries.push_back(a.q);
+    }
+    uint32_t *off = nullptr, *nb = nullptr, n = 0;
+    uint64_t nnz = 0;
+    if (sge_load_graph_file(a.d.c_str(), &off, &nb, &n, &nnz) != SGE_OK) {
+        std::cout << sge_last_error() << std::endl;
+        return 1;
+    }
+    sge_graph *g = nullptr;
+    if (sge_graph_create(off, nb, n, nnz, a.device, &g) != SGE_OK) {
+        std::cout << "error: " << sge_last_error() << std::endl;
+        return 1;
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<sge_plan *> plans;
+    std::vector<sge_plan_blob> blobs;
+    for (auto &qp : queries) {
+        uint32_t k, m, edges[2 * SGE_MAX_K * SGE_MAX_K];
+        if (sge_load_pattern_file(qp.c_str(), &k, &m, edges) != SGE_OK) {
+            std::cout << sge_last_error() << std::endl;
+            return 1;
+        }
+        sge_plan_opts po{};
+        po.join_style = a.explore ? SGE_JOIN_EXPLORATION : SGE_JOIN_WCOJ;
+        po.use_iep = a.iep ? 1u : 0u;
+        po.max_tail = SGE_MAX_TAIL;
+        po.seed = a.seed;
+        sge_plan_blob b;
+        if (sge_plan_pattern(k, m, edges, g, &po, &b) != SGE_OK) {
+            std::cout << "error: " << sge_last_error() << std::endl;
+            return 1;
+        }
+        sge_plan *p = nullptr;
+        if (sge_plan_create(&b, &p) != SGE_OK) {
+            std::cout << "error: " << sge_last_error() << std::endl;
+            return 1;
+        }
+        blobs.push_back(b);
+        plans.push_back(p);
+    }
+    double plan_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    for (size_t i = 0; i < blobs.size(); ++i) {
+        const sge_plan_blob &b = blobs[i];
+        out << "num bags: " << (b.single_bag ? 1 : 2) << std::endl;
+        out << "matching order:";
+        for (uint32_t l = 0; l < b.k; ++l) out << (l ? "," : " ") << b.order[l];
+        out << std::endl;
+    }
+    out << "Planning time (s): " << plan_s << std::endl;
+    out << "traverse all level: 0" << std::endl;
+    out << "use iep: " << (a.iep ? 1 : 0) << std::endl;
+    if (a.threads > 1) out << "Number of threads: " << a.threads << std::endl;
+    bool optimized = false;
+    for (auto &b : blobs) optimized |= b.tail_len > 1;
+    if (a.iep && optimized) out << "optimized traversal" << std::endl;
+    std::vector<uint64_t> counts(plans.size()), inst(plans.size());
+    sge_stats st{};
+    auto t1 = std::chrono::steady_clock::now();
+    sge_status s = sge_count(g, plans.data(), (uint32_t)plans.size(), nullptr, counts.data(), inst.data(), &st);
+    double exec_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
+    if (s != SGE_OK) {
+        std::cout << "error: " << sge_last_error() << std::endl;
+        return 1;
+    }
+    for (size_t i = 0; i < plans.size(); ++i) {
+        if (plans.size() > 1) out << "pattern: " << queries[i] << std::endl;
+        out << "Number of matches: " << counts[i] << std::endl;
+        out << "Number of instances: " << inst[i] << std::endl;
+    }
+    out << "Number of intersections: " << st.set_ops << std::endl;
+    out << "Execution Time: " << exec_s << std::endl;
+    out << "GPU time (ms): " << st.kernel_ms << std::endl;
+    for (auto *p : plans) sge_plan_destroy(p);
+    sge_graph_destroy(g);
+    sge_free_host(off);
+    sge_free_host(nb);
+    return 0;
+}

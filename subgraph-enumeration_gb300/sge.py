@@ -1,0 +1,399 @@
+"""Python mirror of the libsge C ABI (include/sge.h), shaped like the
+reference's own entry points so callers and tests read like the reference:
+
+  reference (C++)                                  here
+  ---------------------------------------------    ----------------------------------------
+  DataGraph::loadDataGraph (relation/graph.cpp:255) DataGraph.load(path)
+  PatternGraph::loadPatternGraph (graph.cpp:661)    PatternGraph.load(path)
+  optCostPlan + selectSymmetry + buildTraverse…     plan(pattern, graph, iep=, exploration=)
+    (main.cpp:60-69)
+  sharedJoin / parSharedJoin (main.cpp:86,192)      Engine(graph).count(plans)
+  singleThreadMatch / parallelMatch (main.cpp:12,114) match(query_path, data_path, iep=, exploration=)
+
+The compute path is libsge.so (CUDA kernels for sm_103a).  There is no CPU
+fallback: if the library or a GPU is missing, calls raise SgeError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_build" / "libsge.so"
+CLI_PATH = _PKG / "_build" / "graph_mining_system"
+
+SGE_MAX_K = 16
+SGE_MAX_TAIL = 4
+SGE_MAX_PARTITIONS = 15
+
+STATUS = {0: "OK", 1: "BAD_INPUT", 2: "OOM", 3: "TIMEOUT", 4: "STACK_OVERFLOW", 5: "CUDA_ERROR",
+          6: "UNSUPPORTED", 7: "IO_ERROR", 8: "NO_DEVICE"}
+TAIL_SINGLE, TAIL_CHOOSE, TAIL_IEP = 1, 2, 3
+JOIN_WCOJ, JOIN_EXPLORATION = 0, 1
+
+u32, i32, u64 = C.c_uint32, C.c_int32, C.c_uint64
+
+
+class SgeError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+        self.status_name = STATUS.get(status, str(status))
+
+
+class PlanBlob(C.Structure):
+    _fields_ = [
+        ("magic", u32), ("abi_version", u32), ("k", u32), ("num_enum", u32), ("tail_mode", u32),
+        ("tail_len", u32), ("join_style", u32), ("root_kind", u32),
+        ("order", u32 * SGE_MAX_K), ("parents", u32 * SGE_MAX_K), ("lower", u32 * SGE_MAX_K),
+        ("upper", u32 * SGE_MAX_K), ("check", u32 * SGE_MAX_K), ("base", i32 * SGE_MAX_K),
+        ("rest", u32 * SGE_MAX_K), ("first_parent", u32 * SGE_MAX_K),
+        ("num_partitions", u32), ("part_coef", i32 * SGE_MAX_PARTITIONS),
+        ("part_nblocks", u32 * SGE_MAX_PARTITIONS), ("part_block", (u32 * SGE_MAX_TAIL) * SGE_MAX_PARTITIONS),
+        ("count_multiplier", u64), ("aut_size", u64), ("single_bag", u32), ("num_restrictions", u32),
+        ("est_cost", C.c_double),
+    ]
+
+    def summary(self) -> dict:
+        return {"k": self.k, "order": list(self.order[: self.k]), "num_enum": self.num_enum,
+                "tail_len": self.tail_len, "tail_mode": self.tail_mode, "join_style": self.join_style,
+                "root_kind": self.root_kind, "single_bag": self.single_bag, "aut_size": self.aut_size,
+                "count_multiplier": self.count_multiplier, "est_cost": self.est_cost}
+
+    def to_bytes(self) -> bytes:
+        return bytes(memoryview(self))
+
+    @classmethod
+    def from_bytes(cls, b: bytes) -> "PlanBlob":
+        return cls.from_buffer_copy(b)
+
+
+class PlanOpts(C.Structure):
+    _fields_ = [("join_style", u32), ("use_iep", u32), ("max_tail", u32), ("seed", u64),
+                ("force_order", C.POINTER(u32))]
+
+
+class CountOpts(C.Structure):
+    _fields_ = [("blocks_per_sm", u32), ("warps_per_block", u32), ("chunk", u32), ("time_budget_s", C.c_double),
+                ("max_level_capacity", u32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("kernel_ms", C.c_double), ("total_ms", C.c_double), ("root_tasks", u64), ("set_ops", u64),
+                ("alg_bytes", u64), ("partial_matches", u64), ("gpu_launches", u32), ("status_flags", u32)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class GraphStats(C.Structure):
+    _fields_ = [("num_vertices", C.c_double), ("num_directed_edges", C.c_double),
+                ("moments", C.c_double * (SGE_MAX_K + 2)), ("clustering", C.c_double), ("max_degree", C.c_double)]
+
+
+class GraphInfo(C.Structure):
+    _fields_ = [("num_vertices", u32), ("num_directed_edges", u64), ("max_degree", u32), ("device_bytes", u64)]
+
+
+_lib = None
+
+# C-ABI symbols and their signatures (restype, argtypes).
+_P = C.POINTER
+SIGNATURES = {
+    "sge_struct_size": (C.c_size_t, [C.c_int]),
+    "sge_last_error": (C.c_char_p, []),
+    "sge_version": (C.c_char_p, []),
+    "sge_device_count": (C.c_int, []),
+    "sge_load_graph_file": (C.c_int, [C.c_char_p, _P(_P(u32)), _P(_P(u32)), _P(u32), _P(u64)]),
+    "sge_save_graph_binary": (C.c_int, [C.c_char_p, _P(u32), _P(u32), u32]),
+    "sge_load_pattern_file": (C.c_int, [C.c_char_p, _P(u32), _P(u32), _P(u32)]),
+    "sge_csr_from_edges": (C.c_int, [_P(u32), u64, u32, C.c_int, _P(_P(u32)), _P(_P(u32)), _P(u64)]),
+    "sge_free_host": (None, [C.c_void_p]),
+    "sge_gen_rmat": (C.c_int, [u32, u64, u32, u32, u32, u64, _P(_P(u32)), _P(u64)]),
+    "sge_gen_chung_lu": (C.c_int, [u32, u64, u32, u32, u64, _P(_P(u32)), _P(u64)]),
+    "sge_gen_pattern": (C.c_int, [u32, u32, u64, _P(u32)]),
+    "sge_plan_pattern": (C.c_int, [u32, u32, _P(u32), C.c_void_p, _P(PlanOpts), _P(PlanBlob)]),
+    "sge_pattern_info": (C.c_int, [u32, u32, _P(u32), _P(u64), _P(u32)]),
+    "sge_plan_validate": (C.c_int, [_P(PlanBlob)]),
+    "sge_graph_stats_compute": (C.c_int, [_P(u32), _P(u32), u32, _P(GraphStats)]),
+    "sge_plan_pattern_stats": (C.c_int, [u32, u32, _P(u32), _P(GraphStats), _P(PlanOpts), _P(PlanBlob)]),
+    "sge_graph_create": (C.c_int, [_P(u32), _P(u32), u32, u64, C.c_int, _P(C.c_void_p)]),
+    "sge_graph_destroy": (C.c_int, [C.c_void_p]),
+    "sge_graph_get_info": (C.c_int, [C.c_void_p, _P(GraphInfo)]),
+    "sge_plan_create": (C.c_int, [_P(PlanBlob), _P(C.c_void_p)]),
+    "sge_plan_destroy": (C.c_int, [C.c_void_p]),
+    "sge_count": (C.c_int, [C.c_void_p, _P(C.c_void_p), u32, _P(CountOpts), _P(u64), _P(u64), _P(Stats)]),
+    "sge_count_host": (C.c_int, [_P(u32), _P(u32), u32, u64, _P(PlanBlob), u32, _P(CountOpts), _P(u64), _P(Stats)]),
+}
+
+
+def lib() -> C.CDLL:
+    """Loads libsge.so (built by sge_build.build_sge); raises if it is missing."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise SgeError(6, f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(st: int) -> None:
+    if st != 0:
+        raise SgeError(st, lib().sge_last_error().decode(errors="replace"))
+
+
+def _u32p(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(u32))
+
+
+def _take_u32(ptr, n: int) -> np.ndarray:
+    out = np.ctypeslib.as_array(ptr, shape=(max(n, 1),))[:n].copy() if n else np.zeros(0, np.uint32)
+    lib().sge_free_host(C.cast(ptr, C.c_void_p))
+    return out
+
+
+# ---------------------------------------------------------------- graphs ----
+@dataclass
+class DataGraph:
+    """Symmetric CSR with sorted neighbour lists (relation/graph.h:113-213)."""
+    offsets: np.ndarray
+    nbrs: np.ndarray
+
+    @property
+    def num_vertices(self) -> int:
+        return int(self.offsets.shape[0] - 1)
+
+    @property
+    def num_edges(self) -> int:
+        return int(self.nbrs.shape[0] // 2)
+
+    @property
+    def max_degree(self) -> int:
+        return int(np.diff(self.offsets).max()) if self.num_vertices else 0
+
+    @classmethod
+    def load(cls, path: str | os.PathLike) -> "DataGraph":
+        off, nb = C.POINTER(u32)(), C.POINTER(u32)()
+        n, nnz = u32(), u64()
+        _check(lib().sge_load_graph_file(str(path).encode(), C.byref(off), C.byref(nb), C.byref(n), C.byref(nnz)))
+        return cls(_take_u32(off, n.value + 1), _take_u32(nb, nnz.value))
+
+    @classmethod
+    def from_edges(cls, edges: np.ndarray, num_vertices: int, dedup: bool = True) -> "DataGraph":
+        e = np.ascontiguousarray(edges, dtype=np.uint32).reshape(-1)
+        off, nb = C.POINTER(u32)(), C.POINTER(u32)()
+        nnz = u64()
+        _check(lib().sge_csr_from_edges(_u32p(e), e.size // 2, num_vertices, int(dedup), C.byref(off), C.byref(nb),
+                                        C.byref(nnz)))
+        return cls(_take_u32(off, num_vertices + 1), _take_u32(nb, nnz.value))
+
+    def save_binary(self, path: str | os.PathLike) -> None:
+        _check(lib().sge_save_graph_binary(str(path).encode(), _u32p(self.offsets), _u32p(self.nbrs),
+                                           self.num_vertices))
+
+    def save_text(self, path: str | os.PathLike) -> None:
+        src = np.repeat(np.arange(self.num_vertices, dtype=np.uint32), np.diff(self.offsets))
+        keep = src < self.nbrs
+        with open(path, "w") as f:
+            f.write(f"{self.num_vertices} {int(keep.sum())}\n")
+            np.savetxt(f, np.stack([src[keep], self.nbrs[keep]], 1), fmt="%d")
+
+    def stats(self) -> GraphStats:
+        """Planner statistics (degree moments, sampled clustering) on the host."""
+        st = GraphStats()
+        _check(lib().sge_graph_stats_compute(_u32p(np.ascontiguousarray(self.offsets, np.uint32)),
+                                             _u32p(np.ascontiguousarray(self.nbrs, np.uint32)),
+                                             self.num_vertices, C.byref(st)))
+        return st
+
+    def edge_array(self) -> np.ndarray:
+        src = np.repeat(np.arange(self.num_vertices, dtype=np.uint32), np.diff(self.offsets))
+        keep = src < self.nbrs
+        return np.stack([src[keep], self.nbrs[keep]], 1)
+
+    def fingerprint(self) -> str:
+        import hashlib
+        h = hashlib.sha256()
+        h.update(np.ascontiguousarray(self.offsets, np.uint32).tobytes())
+        h.update(np.ascontiguousarray(self.nbrs, np.uint32).tobytes())
+        return h.hexdigest()[:16]
+
+
+@dataclass
+class PatternGraph:
+    """Unlabeled query pattern (relation/graph.h PatternGraph)."""
+    k: int
+    edges: np.ndarray  # (m, 2) uint32
+
+    @property
+    def m(self) -> int:
+        return int(self.edges.shape[0])
+
+    @classmethod
+    def load(cls, path: str | os.PathLike) -> "PatternGraph":
+        k, m = u32(), u32()
+        buf = (u32 * (2 * SGE_MAX_K * SGE_MAX_K))()
+        _check(lib().sge_load_pattern_file(str(path).encode(), C.byref(k), C.byref(m), buf))
+        return cls(k.value, np.array(buf[: 2 * m.value], dtype=np.uint32).reshape(-1, 2))
+
+    @classmethod
+    def from_edges(cls, k: int, edges) -> "PatternGraph":
+        return cls(int(k), np.asarray(edges, dtype=np.uint32).reshape(-1, 2))
+
+    @classmethod
+    def random(cls, k: int, m: int, seed: int) -> "PatternGraph":
+        buf = (u32 * (2 * m))()
+        _check(lib().sge_gen_pattern(k, m, seed, buf))
+        return cls(k, np.array(buf[:], dtype=np.uint32).reshape(-1, 2))
+
+    def flat(self) -> np.ndarray:
+        return np.ascontiguousarray(self.edges, dtype=np.uint32).reshape(-1)
+
+    def info(self) -> tuple[int, bool]:
+        """(|Aut|, single_bag)"""
+        a, s = u64(), u32()
+        e = self.flat()
+        _check(lib().sge_pattern_info(self.k, self.m, _u32p(e), C.byref(a), C.byref(s)))
+        return int(a.value), bool(s.value)
+
+    def text(self) -> str:
+        return f"{self.k} {self.m}\n" + "".join(f"{a} {b}\n" for a, b in self.edges)
+
+
+# ------------------------------------------------------------ generators ----
+def gen_rmat(scale: int, m: int, a: float = 0.57, b: float = 0.19, c: float = 0.19, seed: int = 0) -> DataGraph:
+    ep, mo = C.POINTER(u32)(), u64()
+    _check(lib().sge_gen_rmat(scale, m, round(a * 1e6), round(b * 1e6), round(c * 1e6), seed, C.byref(ep),
+                              C.byref(mo)))
+    e = _take_u32(ep, 2 * mo.value)
+    return DataGraph.from_edges(e, 1 << scale, dedup=False)
+
+
+def gen_chung_lu(n: int, m: int, gamma: float, max_deg: int = 0, seed: int = 0) -> DataGraph:
+    ep, mo = C.POINTER(u32)(), u64()
+    _check(lib().sge_gen_chung_lu(n, m, round(gamma * 1000), max_deg, seed, C.byref(ep), C.byref(mo)))
+    e = _take_u32(ep, 2 * mo.value)
+    return DataGraph.from_edges(e, n, dedup=False)
+
+
+# --------------------------------------------------------------- planner ----
+def plan(pattern: PatternGraph, graph: "Engine | GraphStats | DataGraph | None" = None, iep: bool = True,
+         exploration: bool = False, max_tail: int = SGE_MAX_TAIL, force_order=None, seed: int = 1) -> PlanBlob:
+    """Plans a pattern (the host planning half of graph_mining_system).  The
+    cost model reads the graph's statistics: pass the Engine, a DataGraph, or
+    precomputed GraphStats (None = a generic sparse graph)."""
+    o = PlanOpts(JOIN_EXPLORATION if exploration else JOIN_WCOJ, int(iep), max_tail, seed, None)
+    keep = None
+    if force_order is not None:
+        keep = np.ascontiguousarray(force_order, dtype=np.uint32)
+        o.force_order = _u32p(keep)
+    b = PlanBlob()
+    e = pattern.flat()
+    if isinstance(graph, DataGraph):
+        graph = graph.stats()
+    if isinstance(graph, GraphStats):
+        _check(lib().sge_plan_pattern_stats(pattern.k, pattern.m, _u32p(e), C.byref(graph), C.byref(o), C.byref(b)))
+    else:
+        _check(lib().sge_plan_pattern(pattern.k, pattern.m, _u32p(e), graph._h if graph else None, C.byref(o),
+                                      C.byref(b)))
+    return b
+
+
+def validate_plan(b: PlanBlob) -> None:
+    _check(lib().sge_plan_validate(C.byref(b)))
+
+
+# ---------------------------------------------------------------- engine ----
+class Engine:
+    """A device-resident data graph (sge_graph) plus batched counting."""
+
+    def __init__(self, graph: DataGraph, device: int = 0):
+        self.graph = graph
+        self._off = np.ascontiguousarray(graph.offsets, np.uint32)
+        self._nb = np.ascontiguousarray(graph.nbrs, np.uint32)
+        h = C.c_void_p()
+        _check(lib().sge_graph_create(_u32p(self._off), _u32p(self._nb), graph.num_vertices, self._nb.size, device,
+                                      C.byref(h)))
+        self._h = h
+
+    def info(self) -> dict:
+        gi = GraphInfo()
+        _check(lib().sge_graph_get_info(self._h, C.byref(gi)))
+        return {f: getattr(gi, f) for f, _ in gi._fields_}
+
+    def count(self, plans: list[PlanBlob], stats: bool = False, time_budget_s: float = 0.0,
+              max_level_capacity: int = 0, blocks_per_sm: int = 0, warps_per_block: int = 0, chunk: int = 0):
+        """Counts every plan over the graph in one launch.  Returns (counts,
+        instances, stats-dict or None); counts are the reference's "Number of
+        matches" (uint64)."""
+        handles = []
+        try:
+            for b in plans:
+                ph = C.c_void_p()
+                _check(lib().sge_plan_create(C.byref(b), C.byref(ph)))
+                handles.append(ph)
+            arr = (C.c_void_p * len(handles))(*[h.value for h in handles])
+            counts = (u64 * len(plans))()
+            inst = (u64 * len(plans))()
+            st = Stats()
+            o = CountOpts(blocks_per_sm, warps_per_block, chunk, time_budget_s, max_level_capacity)
+            _check(lib().sge_count(self._h, arr, len(plans), C.byref(o), counts, inst,
+                                   C.byref(st) if stats else None))
+            return list(counts), list(inst), (st.as_dict() if stats else None)
+        finally:
+            for h in handles:
+                lib().sge_plan_destroy(h)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().sge_graph_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def count_host(graph: DataGraph, plans: list[PlanBlob], stats: bool = False):
+    """End-to-end call through sge_count_host: host CSR in, counts out."""
+    arr = (PlanBlob * len(plans))(*plans)
+    counts = (u64 * len(plans))()
+    st = Stats()
+    off = np.ascontiguousarray(graph.offsets, np.uint32)
+    nb = np.ascontiguousarray(graph.nbrs, np.uint32)
+    _check(lib().sge_count_host(_u32p(off), _u32p(nb), graph.num_vertices, nb.size, arr, len(plans), None, counts,
+                                C.byref(st) if stats else None))
+    return list(counts), (st.as_dict() if stats else None)
+
+
+def match(query_path, data_path, iep: bool = False, exploration: bool = False, device: int = 0) -> dict:
+    """singleThreadMatch / parallelMatch (main.cpp:12-218) on the GPU: load,
+    plan, count.  Returns the log fields as a dict."""
+    import time
+    q = PatternGraph.load(query_path)
+    g = DataGraph.load(data_path)
+    with Engine(g, device) as eng:
+        t0 = time.perf_counter()
+        b = plan(q, eng, iep=iep, exploration=exploration)
+        t1 = time.perf_counter()
+        counts, inst, st = eng.count([b], stats=True)
+        t2 = time.perf_counter()
+    return {"Number of matches": counts[0], "Number of instances": inst[0], "Planning time (s)": t1 - t0,
+            "Execution Time": t2 - t1, "Number of intersections": st["set_ops"], "plan": b.summary()}
