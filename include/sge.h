@@ -146,9 +146,14 @@ typedef struct sge_count_opts {
     uint32_t chunk;             /* root tasks per queue grab; 0 = auto */
     double   time_budget_s;     /* 0 = unlimited; otherwise kernels stop and report SGE_TIMEOUT */
     uint32_t max_level_capacity;/* 0 = graph max degree; smaller values exercise the overflow path */
+    uint64_t root_stride;       /* 0/1 = every root task; s > 1: only tasks t ≡ root_offset (mod s) */
+    uint64_t root_offset;       /* (root-range sharding across ranks, or sampled runs) */
+    uint32_t collect_counters;  /* 1: run the instrumented kernel (set_ops, alg_bytes, partial matches) */
 } sge_count_opts;
 
-/* Statistics of one sge_count call (per call, summed over plans) */
+/* Statistics of one sge_count call (per call, summed over plans).  kernel_ms,
+ * total_ms, gpu_launches and status_flags are always filled; the counters
+ * only with sge_count_opts.collect_counters. */
 typedef struct sge_stats {
     double   kernel_ms;         /* device time of the counting kernels (CUDA events) */
     double   total_ms;          /* host wall time of the call */

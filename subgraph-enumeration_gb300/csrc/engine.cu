@@ -56,7 +56,8 @@ struct DevPlan {
     int32_t part_coef[SGE_MAX_PARTITIONS];
     uint32_t part_nblocks[SGE_MAX_PARTITIONS];
     uint32_t part_block[SGE_MAX_PARTITIONS][SGE_MAX_TAIL];
-    unsigned long long task_begin, ntasks;
+    unsigned long long task_begin, ntasks;        // this batch's task range for the plan
+    unsigned long long root_stride, root_offset;  // task j of the plan = root root_offset + j*root_stride
 };
 
 struct DevStats {
@@ -538,7 +539,7 @@ __global__ void __launch_bounds__(256) count_kernel(DevGraph g, const DevPlan *_
                 for (uint32_t w = lane; w < sizeof(DevPlan) / 4; w += 32) dst[w] = src[w];
                 __syncwarp();
             }
-            unsigned long long lt = t - P.task_begin;
+            unsigned long long lt = P.root_offset + (t - P.task_begin) * P.root_stride;
             uint2 e;
             if (P.root_kind == SGE_ROOT_ANY) {
                 e = g.edges[lt >> 1];
@@ -836,7 +837,13 @@ sge_status sge_count(sge_graph *g, const sge_plan *const *plans, uint32_t nplans
         if (!plans[i]) return fail(SGE_BAD_INPUT, "plan %u is null", i);
         dps[i] = plans[i]->dp;
         dps[i].task_begin = total;
-        dps[i].ntasks = (dps[i].root_kind == SGE_ROOT_ANY) ? 2ull * g->m : g->m;
+        const unsigned long long all = (dps[i].root_kind == SGE_ROOT_ANY) ? 2ull * g->m : g->m;
+        const unsigned long long stride = o.root_stride > 1 ? o.root_stride : 1ull;
+        const unsigned long long offs = o.root_offset;
+        if (stride > 1 && offs >= stride) return fail(SGE_BAD_INPUT, "root_offset %llu >= root_stride %llu", offs, stride);
+        dps[i].root_stride = stride;
+        dps[i].root_offset = stride > 1 ? offs : 0;
+        dps[i].ntasks = all > dps[i].root_offset ? (all - dps[i].root_offset + stride - 1) / stride : 0;
         total += dps[i].ntasks;
         nbufs = std::max(nbufs, dps[i].nbufs);
         if (dps[i].k > SGE_MAX_K) return fail(SGE_UNSUPPORTED, "plan %u has k=%u", i, dps[i].k);
@@ -844,7 +851,7 @@ sge_status sge_count(sge_graph *g, const sge_plan *const *plans, uint32_t nplans
     const uint32_t wpb = o.warps_per_block ? std::min<uint32_t>(o.warps_per_block, 8) : 8;
     const uint32_t threads = wpb * 32;
     const size_t smem = sizeof(WarpState) * wpb;
-    const bool want_stats = stats != nullptr;
+    const bool want_stats = o.collect_counters != 0;
     int bps = 0;
     if (want_stats) CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, count_kernel<true>, threads, smem));
     else CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, count_kernel<false>, threads, smem));

@@ -79,7 +79,7 @@ class PlanOpts(C.Structure):
 
 class CountOpts(C.Structure):
     _fields_ = [("blocks_per_sm", u32), ("warps_per_block", u32), ("chunk", u32), ("time_budget_s", C.c_double),
-                ("max_level_capacity", u32)]
+                ("max_level_capacity", u32), ("root_stride", u64), ("root_offset", u64), ("collect_counters", u32)]
 
 
 class Stats(C.Structure):
@@ -331,10 +331,14 @@ class Engine:
         return {f: getattr(gi, f) for f, _ in gi._fields_}
 
     def count(self, plans: list[PlanBlob], stats: bool = False, time_budget_s: float = 0.0,
-              max_level_capacity: int = 0, blocks_per_sm: int = 0, warps_per_block: int = 0, chunk: int = 0):
+              max_level_capacity: int = 0, blocks_per_sm: int = 0, warps_per_block: int = 0, chunk: int = 0,
+              root_stride: int = 1, root_offset: int = 0):
         """Counts every plan over the graph in one launch.  Returns (counts,
-        instances, stats-dict or None); counts are the reference's "Number of
-        matches" (uint64)."""
+        instances, stats-dict); counts are the reference's "Number of matches"
+        (uint64).  stats=True runs the instrumented kernel (set operations,
+        algorithmic bytes); kernel_ms is reported either way.
+        root_stride/root_offset restrict the run to root tasks
+        t ≡ root_offset (mod root_stride) (sharding, sampling)."""
         handles = []
         try:
             for b in plans:
@@ -345,10 +349,10 @@ class Engine:
             counts = (u64 * len(plans))()
             inst = (u64 * len(plans))()
             st = Stats()
-            o = CountOpts(blocks_per_sm, warps_per_block, chunk, time_budget_s, max_level_capacity)
-            _check(lib().sge_count(self._h, arr, len(plans), C.byref(o), counts, inst,
-                                   C.byref(st) if stats else None))
-            return list(counts), list(inst), (st.as_dict() if stats else None)
+            o = CountOpts(blocks_per_sm, warps_per_block, chunk, time_budget_s, max_level_capacity, root_stride,
+                          root_offset, int(stats))
+            _check(lib().sge_count(self._h, arr, len(plans), C.byref(o), counts, inst, C.byref(st)))
+            return list(counts), list(inst), st.as_dict()
         finally:
             for h in handles:
                 lib().sge_plan_destroy(h)
@@ -378,9 +382,10 @@ def count_host(graph: DataGraph, plans: list[PlanBlob], stats: bool = False):
     st = Stats()
     off = np.ascontiguousarray(graph.offsets, np.uint32)
     nb = np.ascontiguousarray(graph.nbrs, np.uint32)
-    _check(lib().sge_count_host(_u32p(off), _u32p(nb), graph.num_vertices, nb.size, arr, len(plans), None, counts,
-                                C.byref(st) if stats else None))
-    return list(counts), (st.as_dict() if stats else None)
+    o = CountOpts(0, 0, 0, 0.0, 0, 1, 0, int(stats))
+    _check(lib().sge_count_host(_u32p(off), _u32p(nb), graph.num_vertices, nb.size, arr, len(plans), C.byref(o),
+                                counts, C.byref(st)))
+    return list(counts), st.as_dict()
 
 
 def match(query_path, data_path, iep: bool = False, exploration: bool = False, device: int = 0) -> dict:

@@ -1,0 +1,45 @@
+"""The graph_mining_system binary keeps the reference's flags and log keys."""
+import re
+import subprocess
+
+import pytest
+
+from conftest import GOLDEN, PKG, pattern_of
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("flags", [[], ["-u"], ["-i"], ["-i", "-u", "-t", "8"]])
+def test_cli_counts(sge, patterns, tmp_path, flags):
+    q = tmp_path / "q.txt"
+    q.write_text(pattern_of(sge, patterns, "light_query/p6").text())
+    out = subprocess.run([str(PKG / "_build" / "graph_mining_system"), "-q", str(q), "-d",
+                          str(GOLDEN / "ca_netscience.el"), *flags], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert re.search(r"Number of matches: 13463\b", out.stdout)
+    for key in ("Planning time (s):", "use iep:", "Execution Time:", "Number of intersections:"):
+        assert key in out.stdout
+
+
+def test_cli_batch_and_result_file(sge, patterns, tmp_path):
+    names = ["light_query/p2", "light_query/p3", "light_query/p4"]
+    paths = []
+    for i, n in enumerate(names):
+        f = tmp_path / f"q{i}.txt"
+        f.write_text(pattern_of(sge, patterns, n).text())
+        paths.append(str(f))
+    lst = tmp_path / "list.txt"
+    lst.write_text("\n".join(paths) + "\n")
+    res = tmp_path / "log.txt"
+    out = subprocess.run([str(PKG / "_build" / "graph_mining_system"), "--batch", str(lst), "-d",
+                          str(GOLDEN / "ca_netscience.el"), "-u", "-r", str(res)], capture_output=True, text=True,
+                         timeout=300)
+    assert out.returncode == 0
+    got = [int(x) for x in re.findall(r"Number of matches: (\d+)", res.read_text())]
+    assert got == [4680, 15144, 36742]
+
+
+def test_cli_missing_file_exits_1(tmp_path):
+    out = subprocess.run([str(PKG / "_build" / "graph_mining_system"), "-q", str(tmp_path / "nope"), "-d",
+                          str(GOLDEN / "ca_netscience.el")], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 1 and "Can not open file" in out.stdout

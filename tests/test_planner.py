@@ -1,0 +1,96 @@
+"""Host planner: count semantics (single-bag vs multi-bag, pinned against the
+reference's "num bags"), plan validity, and the differential planner test:
+different plans of one pattern give the same count."""
+import numpy as np
+import pytest
+
+from conftest import golden_rows, pattern_of
+
+
+def test_single_bag_rule_matches_reference(sge, patterns, golden):
+    seen = set()
+    for r in golden["results"]:
+        if r["num_bags"] is None or r["pattern"] in seen:
+            continue
+        seen.add(r["pattern"])
+        p = pattern_of(sge, patterns, r["pattern"])
+        aut, single = p.info()
+        assert single == (r["num_bags"] == 1), r["pattern"]
+    assert len(seen) > 200
+
+
+def test_every_pattern_plans_and_validates(sge, patterns):
+    for name, pj in patterns.items():
+        p = sge.PatternGraph.from_edges(pj["k"], pj["edges"])
+        for iep in (False, True):
+            for expl in (False, True):
+                b = sge.plan(p, None, iep=iep, exploration=expl)
+                sge.validate_plan(b)
+                assert b.k == p.k
+                assert sorted(b.order[: b.k]) == list(range(p.k))
+                if not iep:
+                    assert b.tail_len == 1
+                assert b.count_multiplier == (b.aut_size if b.single_bag else 1)
+
+
+def test_plan_blob_roundtrip(sge, patterns):
+    p = pattern_of(sge, patterns, "light_query/p4")
+    b = sge.plan(p, None)
+    b2 = sge.PlanBlob.from_bytes(b.to_bytes())
+    assert b2.to_bytes() == b.to_bytes()
+
+
+def test_validate_rejects_corrupt_plans(sge, patterns):
+    p = pattern_of(sge, patterns, "light_query/p4")
+    good = sge.plan(p, None)
+    for mutate in [lambda b: setattr(b, "magic", 0), lambda b: setattr(b, "k", 40),
+                   lambda b: b.parents.__setitem__(2, 0), lambda b: b.check.__setitem__(3, 0),
+                   lambda b: setattr(b, "tail_len", 3), lambda b: setattr(b, "count_multiplier", 0)]:
+        b = sge.PlanBlob.from_bytes(good.to_bytes())
+        mutate(b)
+        with pytest.raises(sge.SgeError):
+            sge.validate_plan(b)
+
+
+def test_bad_patterns(sge):
+    with pytest.raises(sge.SgeError) as e:
+        sge.plan(sge.PatternGraph.from_edges(4, [(0, 1), (2, 3)]), None)
+    assert e.value.status_name == "UNSUPPORTED"
+    with pytest.raises(sge.SgeError):
+        sge.plan(sge.PatternGraph.from_edges(3, [(0, 0), (1, 2)]), None)
+    with pytest.raises(sge.SgeError):
+        sge.plan(sge.PatternGraph.from_edges(17, [(i, i + 1) for i in range(16)]), None)
+
+
+@pytest.mark.parametrize("name", ["light_query/p2", "light_query/p4", "light_query/p5", "light_query/p7",
+                                  "huge_query/p8", "6vertex/3", "7vertex/12", "two_triangles_4cycle"])
+def test_different_plans_same_count(sge, oracle, patterns, golden, graphs, name):
+    """Forced orders × IEP on/off × join style: one count (planner differential test)."""
+    g = graphs("ca_netscience")
+    want = next(r["count"] for r in golden_rows(golden, "ca_netscience") if r["pattern"] == name)
+    p = pattern_of(sge, patterns, name)
+    rng = np.random.default_rng(len(name))
+    tried = 0
+    for _ in range(60):
+        order = rng.permutation(p.k).tolist()
+        for iep in (False, True):
+            try:
+                b = sge.plan(p, None, iep=iep, force_order=order, exploration=bool(tried % 2))
+            except sge.SgeError:
+                break  # not a connected order starting with an edge
+            inst, _ = oracle.count_plan(g.offsets, g.nbrs, b, threads=4)
+            assert inst * b.count_multiplier == want, (order, iep)
+            tried += 1
+        if tried >= 12:
+            break
+    assert tried >= 4
+
+
+def test_iep_tails_are_used(sge, patterns, graphs):
+    st = graphs("ca_netscience").stats()
+    modes = {}
+    for name in ["light_query/p2", "light_query/p4", "7vertex/0"]:
+        b = sge.plan(pattern_of(sge, patterns, name), st, iep=True)
+        modes[name] = (b.tail_mode, b.tail_len)
+    assert modes["light_query/p2"] == (sge.TAIL_CHOOSE, 2)
+    assert modes["light_query/p4"][1] >= 2
