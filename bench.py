@@ -193,23 +193,30 @@ def workload_config():
             "parallelism": "root-edge sharding across ranks"}
 
 
-def cpu_baseline(sge, g, plans, budget_s=12.0):
+def cpu_sample(oracle, g, plans, stride, offset, threads):
+    t0 = time.perf_counter()
+    total = roots = 0
+    for b in plans:
+        inst, done = oracle.count_plan(g.offsets, g.nbrs, b, threads=threads, stride=stride, offset=offset)
+        total += inst * b.count_multiplier
+        roots += done
+    return total, time.perf_counter() - t0, roots
+
+
+def cpu_baseline(sge, g, plans, budget_s=15.0):
+    """The oracle port on all host cores over the same root sample of every
+    plan of the step (every stride-th root edge), stride sized for ~budget_s."""
     sys.path.insert(0, str(REPO / "oracle"))
     import oracle
     threads = os.cpu_count() or 1
-    stride = 256
-    t0 = time.perf_counter()
-    total = 0
-    roots = 0
-    for b in plans:
-        inst, done = oracle.count_plan(g.offsets, g.nbrs, b, threads=threads, stride=stride, offset=7)
-        total += inst * b.count_multiplier
-        roots += done
-        if time.perf_counter() - t0 > budget_s:
-            break
-    dt = time.perf_counter() - t0
+    stride = 8192
+    total, dt, roots = cpu_sample(oracle, g, plans, stride, 7, threads)
+    if dt < budget_s / 4:
+        stride = max(1, int(stride * dt / budget_s) or 1)
+        total, dt, roots = cpu_sample(oracle, g, plans, stride, 7 % stride, threads)
     return {"value": total / dt, "unit": "embeddings/s", "cores": threads, "kind": "port",
-            "sample": f"1/{stride} of the root edges (residue 7) of the step's plans, {roots} roots, {dt:.1f} s"}
+            "sample": f"root edges t = 7 mod {stride} of all {len(plans)} plans of a step ({roots} roots, "
+                      f"{dt:.1f} s); value = embeddings of the sample / its time"}
 
 
 def main():
@@ -219,6 +226,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="sge", choices=["sge", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plans", default="", help="comma-separated subset, e.g. house/wcoj-u (profiling)")
+    ap.add_argument("--per-plan", action="store_true", help="time each plan alone and print one JSON per plan")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -234,6 +243,21 @@ def main():
     g = build_workload(sge)
     eng = sge.Engine(g, device=device)
     plans, names = make_plans(sge, eng)
+    if args.plans:
+        keep = set(args.plans.split(","))
+        sel = [i for i, n in enumerate(names) if n in keep]
+        plans, names = [plans[i] for i in sel], [names[i] for i in sel]
+    if args.per_plan:
+        for b, n in zip(plans, names):
+            eng.count([b])
+            c, _, st = eng.count([b], stats=True)
+            c2, _, st2 = eng.count([b])
+            print(json.dumps({"plan": n, "count": c[0], "kernel_ms": st2["kernel_ms"], "alg_bytes": st["alg_bytes"],
+                              "set_ops": st["set_ops"], "partial_matches": st["partial_matches"],
+                              "roots": st["root_tasks"], "stats_kernel_ms": st["kernel_ms"],
+                              "plan_summary": b.summary()}), flush=True)
+        eng.close()
+        return
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=f"cuda:{device}")
     shard = dict(root_stride=world, root_offset=rank) if world > 1 else {}
 
