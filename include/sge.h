@@ -260,6 +260,33 @@ sge_status sge_count_host(const uint32_t *offsets, const uint32_t *nbrs, uint32_
                           uint64_t num_directed_edges, const sge_plan_blob *blobs, uint32_t nplans,
                           const sge_count_opts *opts, uint64_t *counts, sge_stats *stats);
 
+/* ---- counting without any device allocation ----
+ * No counterpart in the reference.  For callers that must not allocate
+ * device memory after set-up: code running under a host framework that owns
+ * the GPU's memory pool, real-time callers with a fixed memory budget, or
+ * callers between graph-capture boundaries.  The caller owns every input and
+ * output buffer.  The working memory of the launch is a file-scope device
+ * array of SGE_NOALLOC_SCRATCH_BYTES that every GPU which loads the library
+ * keeps until the process exits.
+ *   d_offsets, d_nbrs: device CSR (symmetric, sorted lists, uint32)
+ *   max_degree:        an upper bound on the largest list (a smaller value is
+ *                      reported as SGE_STACK_OVERFLOW, never silently wrong)
+ *   plans:             host plan blobs (at most SGE_NOALLOC_MAX_PLANS)
+ *   d_counts:          device uint64[nplans]; receives "Number of matches"
+ *   stream:            a cudaStream_t (NULL = the default stream)
+ * The call is synchronous on `stream` (it reads back the status).  The first
+ * call on a device looks up the array's device address with that device
+ * current; make that first call before any stream capture.  All calls share
+ * the one array, so calls whose launches overlap on the GPU race: serialise
+ * them (one stream, or one call at a time per device).  A graph or plan batch
+ * whose per-warp lists do not fit in the array is rejected with
+ * SGE_UNSUPPORTED. */
+#define SGE_NOALLOC_SCRATCH_BYTES (32u << 20)
+#define SGE_NOALLOC_MAX_PLANS 64u
+sge_status sge_count_noalloc(const uint32_t *d_offsets, const uint32_t *d_nbrs, uint32_t num_vertices,
+                             uint64_t num_directed_edges, uint32_t max_degree, const sge_plan_blob *plans,
+                             uint32_t nplans, uint64_t *d_counts, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -26,6 +26,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -950,3 +951,153 @@ sge_status sge_count_host(const uint32_t *offsets, const uint32_t *nbrs, uint32_
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Counting without device allocation (sge_count_noalloc)
+// ---------------------------------------------------------------------------
+// The launch's working memory lives in one file-scope device array: a header
+// (queue counter, flags), the plan table, then the per-warp candidate lists.
+// Host code must not use the array's name as an address (it is a host-side
+// stand-in); the device address is looked up once per device with that device
+// current (cudaGetSymbolAddress) and passed to the kernel.
+namespace {
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[SGE_NOALLOC_SCRATCH_BYTES];
+
+constexpr size_t NOALLOC_HDR = 256;  // queue (u64) + flags (u32)
+constexpr size_t NOALLOC_PLANS = (sizeof(DevPlan) * SGE_NOALLOC_MAX_PLANS + 255) & ~(size_t)255;
+constexpr size_t NOALLOC_LISTS = NOALLOC_HDR + NOALLOC_PLANS;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+// Root tasks are the directed edges e of the CSR (source found by binary
+// search on the offsets); ASC/DESC plans skip the half with the wrong orientation.
+__global__ void __launch_bounds__(256) count_kernel_noalloc(DevGraph g, const DevPlan *__restrict__ plans,
+                                                            uint32_t nplans, unsigned long long nnz,
+                                                            unsigned long long *queue,
+                                                            unsigned long long *counts, uint32_t *lists,
+                                                            uint32_t cap, uint32_t bufs_per_warp, uint32_t chunk,
+                                                            uint32_t *flags) {
+    extern __shared__ unsigned char smem_raw[];
+    const uint32_t lane = lane_id();
+    const uint32_t wib = threadIdx.x >> 5;
+    WarpState &W = reinterpret_cast<WarpState *>(smem_raw)[wib];
+    __shared__ DevPlan Psh[8];
+    DevPlan &P = Psh[wib];
+    const size_t gwarp = (size_t)blockIdx.x * (blockDim.x >> 5) + wib;
+    Ctx<false> c;
+    c.g = g;
+    c.buf = lists + gwarp * (size_t)bufs_per_warp * cap;
+    c.cap = cap;
+    c.flags = flags;
+    c.set_ops = c.alg_bytes = c.partial = 0;
+    const unsigned long long total = nnz * nplans;
+    int cur = -1;
+    unsigned long long acc = 0;
+    while (true) {
+        unsigned long long t0 = 0;
+        if (lane == 0) t0 = atomicAdd(queue, (unsigned long long)chunk);
+        t0 = __shfl_sync(FULL_MASK, t0, 0);
+        if (t0 >= total) break;
+        if (*(volatile uint32_t *)flags & FLAG_OVERFLOW) break;
+        const unsigned long long t1 = min(t0 + chunk, total);
+        for (unsigned long long t = t0; t < t1; ++t) {
+            const int pi = (int)(t / nnz);
+            if (pi != cur) {
+                if (cur >= 0 && lane == 0 && acc) atomicAdd(counts + cur, acc * P.task_begin);
+                acc = 0;
+                cur = pi;
+                __syncwarp();
+                const uint32_t *src = reinterpret_cast<const uint32_t *>(plans + cur);
+                uint32_t *dst = reinterpret_cast<uint32_t *>(&P);
+                for (uint32_t w = lane; w < sizeof(DevPlan) / 4; w += 32) dst[w] = src[w];
+                __syncwarp();
+            }
+            const uint32_t e = (uint32_t)(t - (unsigned long long)pi * nnz);
+            const uint32_t u = ub(g.off, g.n + 1, e) - 1;  // source of directed edge e
+            const uint32_t v = g.adj[e];
+            if (P.root_kind == SGE_ROOT_ASC && !(u < v)) continue;
+            if (P.root_kind == SGE_ROOT_DESC && !(u > v)) continue;
+            acc += run_root<false>(P, W, c, u, v);
+        }
+    }
+    // P.task_begin carries the plan's count multiplier in this variant
+    if (cur >= 0 && lane == 0 && acc) atomicAdd(counts + cur, acc * P.task_begin);
+}
+
+}  // namespace
+
+extern "C" sge_status sge_count_noalloc(const uint32_t *d_offsets, const uint32_t *d_nbrs, uint32_t n, uint64_t nnz,
+                                        uint32_t max_degree, const sge_plan_blob *plans, uint32_t nplans,
+                                        uint64_t *d_counts, void *stream_) {
+    if (!d_offsets || (!d_nbrs && nnz) || (!plans && nplans) || (!d_counts && nplans))
+        return fail(SGE_BAD_INPUT, "sge_count_noalloc: null argument");
+    if (nplans == 0) return SGE_OK;
+    if (nplans > SGE_NOALLOC_MAX_PLANS)
+        return fail(SGE_UNSUPPORTED, "sge_count_noalloc: %u plans (limit %u)", nplans, SGE_NOALLOC_MAX_PLANS);
+    if (nnz >= (1ull << 32)) return fail(SGE_BAD_INPUT, "%llu directed edges exceed the uint32 EdgeID range", (unsigned long long)nnz);
+    cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return fail(SGE_UNSUPPORTED, "device %d beyond the set-up table", dev);
+    void *base = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p)
+                return fail(SGE_CUDA_ERROR, "cudaGetSymbolAddress(static scratch) on device %d: %s", dev,
+                            cudaGetErrorString(e));
+            g_noalloc_ptr[dev] = p;
+        }
+        base = g_noalloc_ptr[dev];
+    }
+    // plans: validate, convert, copy into the array's plan table
+    uint32_t nbufs = 1;
+    for (uint32_t i = 0; i < nplans; ++i) {
+        sge_status st = sge_plan_validate(&plans[i]);
+        if (st != SGE_OK) return st;
+        DevPlan dp;
+        to_devplan(plans[i], dp);
+        dp.task_begin = plans[i].count_multiplier;  // multiplier, applied at the atomic flush
+        dp.ntasks = nnz;
+        dp.root_stride = 1;
+        dp.root_offset = 0;
+        nbufs = std::max(nbufs, dp.nbufs);
+        CUDA_TRY(cudaMemcpyAsync(static_cast<unsigned char *>(base) + NOALLOC_HDR + i * sizeof(DevPlan), &dp,
+                                 sizeof(DevPlan), cudaMemcpyHostToDevice, stream));
+    }
+    const uint32_t cap = (std::max<uint32_t>(max_degree, 1) + 31) & ~31u;
+    const size_t per_warp = (size_t)nbufs * cap * sizeof(uint32_t);
+    const size_t avail = SGE_NOALLOC_SCRATCH_BYTES - NOALLOC_LISTS;
+    const uint32_t wpb = 8, threads = wpb * 32;
+    const size_t smem = sizeof(WarpState) * wpb;
+    size_t max_blocks = avail / (per_warp * wpb);
+    if (max_blocks == 0)
+        return fail(SGE_UNSUPPORTED,
+                    "sge_count_noalloc: %u levels x max degree %u need %zu bytes per 8-warp block; the static "
+                    "scratch holds %zu", nbufs, max_degree, per_warp * wpb, avail);
+    int bps = 0, sms = 0;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, count_kernel_noalloc, threads, smem));
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const size_t blocks = std::max<size_t>(1, std::min<size_t>(max_blocks, (size_t)std::max(bps, 1) * sms));
+    // clear what must start at zero: queue, flags, and the caller's counts
+    CUDA_TRY(cudaMemsetAsync(base, 0, NOALLOC_HDR, stream));
+    CUDA_TRY(cudaMemsetAsync(d_counts, 0, sizeof(uint64_t) * nplans, stream));
+    DevGraph dg{d_offsets, d_nbrs, nullptr, n, nnz / 2};
+    unsigned char *B = static_cast<unsigned char *>(base);
+    count_kernel_noalloc<<<(unsigned)blocks, threads, smem, stream>>>(
+        dg, reinterpret_cast<const DevPlan *>(B + NOALLOC_HDR), nplans, nnz,
+        reinterpret_cast<unsigned long long *>(B), reinterpret_cast<unsigned long long *>(d_counts),
+        reinterpret_cast<uint32_t *>(B + NOALLOC_LISTS), cap, nbufs, 4, reinterpret_cast<uint32_t *>(B + 8));
+    CUDA_TRY(cudaGetLastError());
+    uint32_t flags = 0;
+    CUDA_TRY(cudaMemcpyAsync(&flags, B + 8, sizeof flags, cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    if (flags & FLAG_OVERFLOW)
+        return fail(SGE_STACK_OVERFLOW, "a candidate list exceeded max_degree %u (pass a true upper bound)", max_degree);
+    return SGE_OK;
+}

@@ -128,6 +128,8 @@ SIGNATURES = {
     "sge_plan_destroy": (C.c_int, [C.c_void_p]),
     "sge_count": (C.c_int, [C.c_void_p, _P(C.c_void_p), u32, _P(CountOpts), _P(u64), _P(u64), _P(Stats)]),
     "sge_count_host": (C.c_int, [_P(u32), _P(u32), u32, u64, _P(PlanBlob), u32, _P(CountOpts), _P(u64), _P(Stats)]),
+    "sge_count_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, u32, u64, u32, _P(PlanBlob), u32, C.c_void_p,
+                                    C.c_void_p]),
 }
 
 
