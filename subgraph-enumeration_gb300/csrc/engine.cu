@@ -59,6 +59,10 @@ struct DevPlan {
     uint32_t part_block[SGE_MAX_PARTITIONS][SGE_MAX_TAIL];
     unsigned long long task_begin, ntasks;        // this batch's task range for the plan
     unsigned long long root_stride, root_offset;  // task j of the plan = root root_offset + j*root_stride
+    unsigned long long mult;                      // count multiplier (|Aut| for single-bag plans)
+    uint32_t chunk;                               // root tasks per queue grab
+    uint32_t pin_mask;                            // levels 0/1 whose lists are pinned in shared memory
+    uint32_t keep_full;                           // levels whose bound-free list later levels reuse
 };
 
 struct DevStats {
@@ -68,14 +72,34 @@ struct DevStats {
 // Flags written by kernels (never trapped on): bit0 overflow, bit1 timeout.
 enum { FLAG_OVERFLOW = 1u, FLAG_TIMEOUT = 2u };
 
+// Per-warp DFS state (shared memory).
 struct WarpState {
     uint32_t m[SGE_MAX_K];
     uint32_t pos[SGE_MAX_K];
     uint32_t cnt[SGE_MAX_K];
     const uint32_t *list[SGE_MAX_K];
+    const uint32_t *flist[SGE_MAX_K];     // level's full (bound-free) list, for reuse by later levels
+    uint32_t fcnt[SGE_MAX_K];
+    const uint32_t *lptr[SGE_MAX_K];      // N(m[j]) of the matched levels
+    uint32_t llen[SGE_MAX_K];
     uint32_t vlen[SGE_MAX_K][SGE_MAX_K];  // exploration version lengths (j, i)
-    unsigned long long S[16];
+    uint32_t pmode[3];                    // pinned N(m[0]), N(m[1]), level-2 list: 0 none, 1 bitmap, 2 hash
 };
+
+// Leaf state (shared memory): up to 32 candidates of the last enumerated
+// level, each with its own matched values for the levels from L0 on.
+struct LeafState {
+    uint32_t cm[32][2];
+    const uint32_t *cptr[32][2];
+    uint32_t clen[32][2];
+    const uint32_t *bptr[32];
+    uint32_t blen[32];
+    int32_t bsrc[32];
+    uint32_t pref[32];
+    uint32_t cnt[32][16];
+};
+
+constexpr uint32_t PIN_EMPTY = 0xFFFFFFFFu;
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
     unsigned long long t;
@@ -119,6 +143,12 @@ __device__ __forceinline__ unsigned long long binom_exact(unsigned long long n, 
     return (unsigned long long)acc;
 }
 
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);
+    return v;
+}
+
 // Bounds of level i from the current partial match: keep lo < x < hi.
 struct Bounds {
     uint32_t lo, hi;
@@ -159,34 +189,135 @@ struct Ctx {
     uint32_t *buf;    // this warp's scratch: nbufs × cap
     uint32_t cap;
     uint32_t *flags;
+    uint32_t *tab;    // this warp's three pinned-list tables (shared memory), tw words each
+    uint32_t tw;
+    uint32_t tmode;   // 0 none, 1 bitmap over all vertices, 2 open-addressing hash
+    LeafState *L;
     unsigned long long set_ops, alg_bytes, partial;
 };
 
-// Base list of level i for WCOJ: a reused stored list or the smallest parent
-// list; `rest` returns the parents still to test.
+// Membership in a pinned table.
+__device__ __forceinline__ bool pin_has(const uint32_t *t, uint32_t mode, uint32_t tw, uint32_t y) {
+    if (mode == 1) return (t[y >> 5] >> (y & 31u)) & 1u;
+    uint32_t h = (y * 2654435761u) & (tw - 1u);
+    while (true) {  // load factor <= 1/2: an empty slot always ends the probe
+        uint32_t k = t[h];
+        if (k == y) return true;
+        if (k == PIN_EMPTY) return false;
+        h = (h + 1u) & (tw - 1u);
+    }
+}
+
+// y ∈ N(m[j]) for a shared level j (pinned table when present).
+template <bool STATS>
+__device__ __forceinline__ bool in_level_list(const WarpState &W, const Ctx<STATS> &c, uint32_t j, uint32_t y) {
+    if (j < 2 && W.pmode[j]) return pin_has(c.tab + j * c.tw, W.pmode[j], c.tw, y);
+    return contains(W.lptr[j], W.llen[j], y);
+}
+
+// Approximate probe cost of a shared level's list (for choosing base lists).
+__device__ __forceinline__ uint32_t probe_cost(const WarpState &W, uint32_t j, uint32_t len) {
+    if (j < 2 && W.pmode[j]) return 1u;
+    return 2u + (31u - __clz(len + 1u));
+}
+
+// Pins a sorted list into table ti (a bitmap over all vertices, or an
+// open-addressing hash when it is at most half full); records the mode.
+template <bool STATS>
+__device__ void pin_list(WarpState &W, Ctx<STATS> &c, uint32_t ti, const uint32_t *p, uint32_t len) {
+    const uint32_t lane = lane_id();
+    uint32_t mode = c.tmode;
+    if (mode == 2 && len * 2u > c.tw) mode = 0;
+    uint32_t *t = c.tab + ti * c.tw;
+    if (mode == 1) {
+        for (uint32_t e = lane; e < len; e += 32) { uint32_t y = p[e]; atomicOr(&t[y >> 5], 1u << (y & 31u)); }
+    } else if (mode == 2) {
+        for (uint32_t e = lane; e < len; e += 32) {
+            uint32_t y = p[e], h = (y * 2654435761u) & (c.tw - 1u);
+            while (true) {
+                uint32_t old = atomicCAS(&t[h], PIN_EMPTY, y);
+                if (old == PIN_EMPTY || old == y) break;
+                h = (h + 1u) & (c.tw - 1u);
+            }
+        }
+    }
+    if (STATS && mode) c.alg_bytes += 4ull * len;
+    __syncwarp();
+    if (lane == 0) W.pmode[ti] = mode;
+    __syncwarp();
+}
+
+template <bool STATS>
+__device__ void unpin_list(WarpState &W, Ctx<STATS> &c, uint32_t ti, const uint32_t *p, uint32_t len) {
+    const uint32_t lane = lane_id();
+    const uint32_t mode = W.pmode[ti];
+    uint32_t *t = c.tab + ti * c.tw;
+    if (mode == 1) {
+        if (len * 2u < c.tw) {
+            for (uint32_t e = lane; e < len; e += 32) { uint32_t y = p[e]; atomicAnd(&t[y >> 5], ~(1u << (y & 31u))); }
+        } else {
+            for (uint32_t w = lane; w < c.tw; w += 32) t[w] = 0u;
+        }
+    } else if (mode == 2) {
+        for (uint32_t w = lane; w < c.tw; w += 32) t[w] = PIN_EMPTY;
+    }
+    __syncwarp();
+    if (lane == 0) W.pmode[ti] = 0;
+    __syncwarp();
+}
+
+// Pins N(m[0]) and N(m[1]) (levels probed inside the DFS).
+template <bool STATS>
+__device__ void pin_root(const DevPlan &P, WarpState &W, Ctx<STATS> &c) {
+    for (uint32_t j = 0; j < 2; ++j)
+        if ((P.pin_mask >> j) & 1u) pin_list(W, c, j, W.lptr[j], W.llen[j]);
+}
+
+template <bool STATS>
+__device__ void unpin_root(const DevPlan &P, WarpState &W, Ctx<STATS> &c) {
+    for (uint32_t j = 0; j < 2; ++j)
+        if (W.pmode[j]) unpin_list(W, c, j, W.lptr[j], W.llen[j]);
+    if (W.pmode[2]) unpin_list(W, c, 2, W.flist[2], W.fcnt[2]);
+}
+
+__device__ __forceinline__ void set_match(const DevGraph &g, WarpState &W, uint32_t lv, uint32_t x) {
+    // all lanes compute; lane 0 stores
+    const uint32_t *p;
+    uint32_t len;
+    nbr(g, x, p, len);
+    __syncwarp();
+    if (lane_id() == 0) { W.m[lv] = x; W.lptr[lv] = p; W.llen[lv] = len; }
+    __syncwarp();
+}
+
+// Base list of level i for WCOJ: a reused stored list, or the parent list that
+// is cheapest to scan while probing the others; `rest` returns the parents
+// still to test.
 template <bool STATS>
 __device__ __forceinline__ void wcoj_base(const DevPlan &P, const WarpState &W, Ctx<STATS> &c, uint32_t i,
                                           const uint32_t *&bp, uint32_t &blen, uint32_t &rest) {
     if (P.base[i] >= 0) {
         uint32_t l = (uint32_t)P.base[i];
-        bp = W.list[l];
-        blen = W.cnt[l];
+        bp = W.flist[l];
+        blen = W.fcnt[l];
         rest = P.rest[i];
-    } else {
-        uint32_t best = 0, bestlen = 0xFFFFFFFFu;
-        const uint32_t *bestp = nullptr;
-        for (uint32_t msk = P.parents[i]; msk; msk &= msk - 1) {
-            uint32_t j = __ffs(msk) - 1;
-            const uint32_t *p;
-            uint32_t len;
-            nbr(c.g, W.m[j], p, len);
-            if (STATS) c.alg_bytes += 8;
-            if (len < bestlen) { bestlen = len; bestp = p; best = j; }
-        }
-        bp = bestp;
-        blen = bestlen;
-        rest = P.parents[i] & ~(1u << best);
+        return;
     }
+    uint32_t best = 0;
+    unsigned long long bestcost = ~0ull;
+    for (uint32_t msk = P.parents[i]; msk; msk &= msk - 1) {
+        uint32_t j = __ffs(msk) - 1;
+        unsigned long long probes = 0;
+        for (uint32_t o = P.parents[i] & ~(1u << j); o; o &= o - 1) {
+            uint32_t q = __ffs(o) - 1;
+            probes += probe_cost(W, q, W.llen[q]);
+        }
+        unsigned long long cost = (unsigned long long)W.llen[j] * (probes + 1);
+        if (cost < bestcost) { bestcost = cost; best = j; }
+    }
+    bp = W.lptr[best];
+    blen = W.llen[best];
+    rest = P.parents[i] & ~(1u << best);
 }
 
 // Warp-cooperative filter of [bp, bp+blen) by membership in all parent lists
@@ -196,22 +327,17 @@ template <bool STATS, bool STORE>
 __device__ __forceinline__ uint32_t setop(const DevPlan &P, const WarpState &W, Ctx<STATS> &c, uint32_t i,
                                           const uint32_t *bp, uint32_t blen, uint32_t rest, uint32_t *out) {
     const uint32_t lane = lane_id();
-    const uint32_t *lp[SGE_MAX_K];
-    uint32_t ll[SGE_MAX_K];
-    uint32_t nl = 0;
-    for (uint32_t msk = rest; msk; msk &= msk - 1) {
-        uint32_t j = __ffs(msk) - 1;
-        nbr(c.g, W.m[j], lp[nl], ll[nl]);
-        if (STATS) c.alg_bytes += 8ull + 4ull * ll[nl];
-        ++nl;
+    if (STATS) {
+        c.set_ops += 1;
+        c.alg_bytes += 4ull * blen;
+        for (uint32_t msk = rest; msk; msk &= msk - 1) c.alg_bytes += 8ull + 4ull * W.llen[__ffs(msk) - 1];
     }
-    if (STATS) { c.set_ops += 1; c.alg_bytes += 4ull * blen; }
     uint32_t total = 0;
     for (uint32_t off = 0; off < blen; off += 32) {
         uint32_t idx = off + lane;
         bool ok = idx < blen;
         uint32_t x = ok ? bp[idx] : 0u;
-        for (uint32_t l = 0; l < nl && ok; ++l) ok = contains(lp[l], ll[l], x);
+        for (uint32_t msk = rest; msk && ok; msk &= msk - 1) ok = in_level_list(W, c, __ffs(msk) - 1, x);
         if (ok) ok = !excluded(P, W, i, x);
         uint32_t bal = __ballot_sync(FULL_MASK, ok);
         if (STORE) {
@@ -224,29 +350,35 @@ __device__ __forceinline__ uint32_t setop(const DevPlan &P, const WarpState &W, 
 }
 
 // Builds level i's candidate list (WCOJ).  Returns false on overflow.
+// A level that later levels reuse keeps its full intersection (bounds not
+// applied); its own iteration range is that list trimmed by its bounds.
 template <bool STATS>
 __device__ __forceinline__ bool build_level_wcoj(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32_t i) {
     const uint32_t *bp;
     uint32_t blen, rest;
     wcoj_base(P, W, c, i, bp, blen, rest);
-    Bounds b = level_bounds(P, W, i);
-    trim(bp, blen, b);
-    if (rest == 0) {
-        // the base list itself (exclusions are applied while iterating)
-        __syncwarp();
-        if (lane_id() == 0) { W.list[i] = bp; W.cnt[i] = blen; }
-        __syncwarp();
-        return true;
+    const Bounds b = level_bounds(P, W, i);
+    const bool keep = (P.keep_full >> i) & 1u;
+    if (!keep) trim(bp, blen, b);
+    const uint32_t *fp = bp;
+    uint32_t fl = blen;
+    if (rest != 0) {
+        uint32_t *out = c.buf + (size_t)i * c.cap;
+        uint32_t n = setop<STATS, true>(P, W, c, i, bp, blen, rest, out);
+        if (n > c.cap) {
+            if (lane_id() == 0) atomicOr(c.flags, FLAG_OVERFLOW);
+            return false;
+        }
+        fp = out;
+        fl = n;
     }
-    uint32_t *out = c.buf + (size_t)i * c.cap;
-    uint32_t n = setop<STATS, true>(P, W, c, i, bp, blen, rest, out);
+    // (a list taken without intersection keeps the exclusions for iteration time)
+    const uint32_t *ip = fp;
+    uint32_t il = fl;
+    if (keep) trim(ip, il, b);
     __syncwarp();
-    if (lane_id() == 0) { W.list[i] = out; W.cnt[i] = n; }
+    if (lane_id() == 0) { W.flist[i] = fp; W.fcnt[i] = fl; W.list[i] = ip; W.cnt[i] = il; }
     __syncwarp();
-    if (n > c.cap) {
-        if (lane_id() == 0) atomicOr(c.flags, FLAG_OVERFLOW);
-        return false;
-    }
     return true;
 }
 
@@ -255,13 +387,13 @@ template <bool STATS>
 __device__ __forceinline__ const uint32_t *version_ptr(const DevPlan &P, const WarpState &W, const Ctx<STATS> &c,
                                                        uint32_t j, uint32_t i) {
     int s = P.slot[j][i];
-    if (s < 0) return c.g.adj + __ldg(c.g.off + W.m[j]);
+    if (s < 0) return W.lptr[j];
     return c.buf + (size_t)s * c.cap;
 }
 
 // Exploration: after level j is matched, intersect N(m[j]) into the running
 // list of every later level that has j as a parent.  false = prune (empty) or
-// overflow.
+// overflow.  Levels past `upto` are left to the leaf.
 template <bool STATS>
 __device__ __forceinline__ bool explore_update(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32_t j) {
     const uint32_t lane = lane_id();
@@ -269,34 +401,28 @@ __device__ __forceinline__ bool explore_update(const DevPlan &P, WarpState &W, C
         uint32_t i = __ffs(msk) - 1;
         uint32_t below = P.parents[i] & ((1u << j) - 1u);
         if (below == 0) {
-            uint32_t a = __ldg(c.g.off + W.m[j]), bnd = __ldg(c.g.off + W.m[j] + 1);
-            if (STATS) c.alg_bytes += 8;
             __syncwarp();
-            if (lane == 0) W.vlen[j][i] = bnd - a;
+            if (lane == 0) W.vlen[j][i] = W.llen[j];
             __syncwarp();
-            if (bnd == a) return false;
+            if (W.llen[j] == 0) return false;
             continue;
         }
         uint32_t pj = 31 - __clz(below);  // previous parent of i
         const uint32_t *prev = version_ptr(P, W, c, pj, i);
         uint32_t plen = W.vlen[pj][i];
-        const uint32_t *np;
-        uint32_t nl;
-        nbr(c.g, W.m[j], np, nl);
         uint32_t *out = c.buf + (size_t)P.slot[j][i] * c.cap;
-        if (STATS) { c.set_ops += 1; c.alg_bytes += 8ull + 4ull * (plen + nl); }
+        if (STATS) { c.set_ops += 1; c.alg_bytes += 8ull + 4ull * (plen + W.llen[j]); }
         uint32_t total = 0;
-        // probe the longer list with the shorter one
-        const bool swap = nl < plen;
-        const uint32_t *sp = swap ? np : prev;
-        uint32_t sl = swap ? nl : plen;
-        const uint32_t *lp = swap ? prev : np;
-        uint32_t ll = swap ? plen : nl;
+        // scan the running list, probe N(m[j]) (pinned table when present)
+        const bool pinned = j < 2 && W.pmode[j];
+        const bool scan_prev = pinned || plen <= W.llen[j];
+        const uint32_t *sp = scan_prev ? prev : W.lptr[j];
+        const uint32_t sl = scan_prev ? plen : W.llen[j];
         for (uint32_t off = 0; off < sl; off += 32) {
             uint32_t idx = off + lane;
             bool ok = idx < sl;
             uint32_t x = ok ? sp[idx] : 0u;
-            if (ok) ok = contains(lp, ll, x);
+            if (ok) ok = scan_prev ? in_level_list(W, c, j, x) : contains(prev, plen, x);
             uint32_t bal = __ballot_sync(FULL_MASK, ok);
             uint32_t p = total + __popc(bal & ((1u << lane) - 1u));
             if (ok && p < c.cap) out[p] = x;
@@ -321,177 +447,378 @@ __device__ __forceinline__ void explore_level(const DevPlan &P, WarpState &W, Ct
     const uint32_t *bp = version_ptr(P, W, c, lastp, i);
     uint32_t blen = W.vlen[lastp][i];
     Bounds b = level_bounds(P, W, i);
-    trim(bp, blen, b);
     __syncwarp();
+    if (lane_id() == 0) { W.flist[i] = bp; W.fcnt[i] = blen; }
+    trim(bp, blen, b);
     if (lane_id() == 0) { W.list[i] = bp; W.cnt[i] = blen; }
     __syncwarp();
 }
 
-// Leaf count of the tail levels [ne, k) for the current partial match.
-template <bool STATS>
-__device__ unsigned long long tail_count(const DevPlan &P, WarpState &W, Ctx<STATS> &c) {
-    const uint32_t lane = lane_id();
-    const uint32_t ne = P.ne, T = P.T;
-    const bool explore = P.join_style == SGE_JOIN_EXPLORATION;
-    const uint32_t passes = (P.tail_mode == SGE_TAIL_IEP) ? T : 1u;
-    for (uint32_t t = 0; t < passes; ++t) {
-        const uint32_t i = ne + t;
-        const uint32_t *bp;
-        uint32_t blen, rest;
-        if (explore) {
-            uint32_t lastp = 31 - __clz(P.parents[i]);
-            bp = version_ptr(P, W, c, lastp, i);
-            blen = W.vlen[lastp][i];
-            rest = 0;
-        } else {
-            wcoj_base(P, W, c, i, bp, blen, rest);
-        }
-        Bounds b = level_bounds(P, W, i);
-        trim(bp, blen, b);
-        // rest lists of t
-        const uint32_t *lp[SGE_MAX_K];
-        uint32_t ll[SGE_MAX_K];
-        uint32_t nl = 0;
-        for (uint32_t msk = rest; msk; msk &= msk - 1) {
-            uint32_t j = __ffs(msk) - 1;
-            nbr(c.g, W.m[j], lp[nl], ll[nl]);
-            if (STATS) c.alg_bytes += 8ull + 4ull * ll[nl];
-            ++nl;
-        }
-        // other tail positions u > t (IEP only)
-        const uint32_t nu = (P.tail_mode == SGE_TAIL_IEP) ? (T - 1 - t) : 0u;
-        Bounds ub_[SGE_MAX_TAIL];
-        const uint32_t *up_[SGE_MAX_TAIL][SGE_MAX_K];
-        uint32_t ul_[SGE_MAX_TAIL][SGE_MAX_K];
-        uint32_t un_[SGE_MAX_TAIL];
-        for (uint32_t q = 0; q < nu; ++q) {
-            const uint32_t u = i + 1 + q;
-            ub_[q] = level_bounds(P, W, u);
-            un_[q] = 0;
-            if (explore) {
-                uint32_t lastp = 31 - __clz(P.parents[u]);
-                up_[q][0] = version_ptr(P, W, c, lastp, u);
-                ul_[q][0] = W.vlen[lastp][u];
-                un_[q] = 1;
-                if (STATS) c.alg_bytes += 4ull * ul_[q][0];
-            } else {
-                for (uint32_t msk = P.parents[u]; msk; msk &= msk - 1) {
-                    uint32_t j = __ffs(msk) - 1;
-                    nbr(c.g, W.m[j], up_[q][un_[q]], ul_[q][un_[q]]);
-                    if (STATS) c.alg_bytes += 8ull + 4ull * ul_[q][un_[q]];
-                    un_[q]++;
-                }
-            }
-        }
-        if (STATS) { c.set_ops += 1; c.alg_bytes += 4ull * blen; }
-        uint32_t cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        for (uint32_t off = 0; off < blen; off += 32) {
-            uint32_t idx = off + lane;
-            bool ok = idx < blen;
-            uint32_t x = ok ? bp[idx] : 0u;
-            for (uint32_t l = 0; l < nl && ok; ++l) ok = contains(lp[l], ll[l], x);
-            if (ok) ok = !excluded(P, W, i, x);
-            if (ok) {
-                uint32_t fm = 0;
-                for (uint32_t q = 0; q < nu; ++q) {
-                    const uint32_t u = i + 1 + q;
-                    bool f = (!ub_[q].has_lo || x > ub_[q].lo) && (!ub_[q].has_hi || x < ub_[q].hi);
-                    for (uint32_t l = 0; l < un_[q] && f; ++l) f = contains(up_[q][l], ul_[q][l], x);
-                    if (f) f = !excluded(P, W, u, x);
-                    fm |= (uint32_t)f << q;
-                }
-#pragma unroll
-                for (uint32_t s = 0; s < 8; ++s) cnt[s] += ((fm & s) == s) ? 1u : 0u;
-            }
-        }
-        const uint32_t nsub = 1u << nu;
-#pragma unroll
-        for (uint32_t s = 0; s < 8; ++s) {
-            uint32_t tot = __reduce_add_sync(FULL_MASK, cnt[s]);
-            if (s < nsub && lane == 0) W.S[(1u << t) | (s << (t + 1))] = tot;
-        }
-    }
-    __syncwarp();
-    unsigned long long r;
-    if (P.tail_mode == SGE_TAIL_SINGLE) {
-        r = W.S[1];
-    } else if (P.tail_mode == SGE_TAIL_CHOOSE) {
-        r = binom_exact(W.S[1], T);
-    } else {
-        r = 0;
-        for (uint32_t p = 0; p < P.nparts; ++p) {
-            unsigned long long term = (unsigned long long)(long long)P.part_coef[p];
-            for (uint32_t bk = 0; bk < P.part_nblocks[p]; ++bk) term *= W.S[P.part_block[p][bk]];
-            r += term;
-        }
-    }
-    __syncwarp();
-    return r;
+// ---------------------------------------------------------------- leaf ----
+// The leaf counts the tail levels [ne, k) for up to 32 candidates of the last
+// enumerated level at once.  The candidates' (base element) work is flattened
+// across the lanes, so a candidate with a long list does not stall the warp,
+// and every probe into the root's lists is a shared-memory table lookup.
+// Candidate l's value of level p is L.cm[l][p-L0] for p >= L0, W.m[p] below.
+
+// List identity used by the leaf for the pinned stored list of level 2
+// (distinct from the level numbers that name CSR lists).
+constexpr int SRC_LEVEL2_LIST = 40;
+
+struct LeafCtx {
+    uint32_t L0;
+    bool explore;  // exploration: shared parents of a tail level are one running list
+};
+
+__device__ __forceinline__ uint32_t cand_val(const WarpState &W, const LeafState &L, const LeafCtx &lc, uint32_t l,
+                                             uint32_t p) {
+    return p >= lc.L0 ? L.cm[l][p - lc.L0] : W.m[p];
 }
 
-// One root edge: DFS over levels 2..ne-1, tail count at the leaves.
+__device__ __forceinline__ Bounds cand_bounds(const DevPlan &P, const WarpState &W, const LeafState &L,
+                                              const LeafCtx &lc, uint32_t l, uint32_t i) {
+    Bounds b;
+    b.lo = 0;
+    b.hi = 0xFFFFFFFFu;
+    b.has_lo = P.lower[i] != 0;
+    b.has_hi = P.upper[i] != 0;
+    for (uint32_t msk = P.lower[i]; msk; msk &= msk - 1) b.lo = max(b.lo, cand_val(W, L, lc, l, __ffs(msk) - 1));
+    for (uint32_t msk = P.upper[i]; msk; msk &= msk - 1) b.hi = min(b.hi, cand_val(W, L, lc, l, __ffs(msk) - 1));
+    return b;
+}
+
+__device__ __forceinline__ bool cand_excluded(const DevPlan &P, const WarpState &W, const LeafState &L,
+                                              const LeafCtx &lc, uint32_t l, uint32_t i, uint32_t y) {
+    bool ex = false;
+    for (uint32_t msk = P.check[i]; msk; msk &= msk - 1) ex |= (cand_val(W, L, lc, l, __ffs(msk) - 1) == y);
+    return ex;
+}
+
+// Visits the lists whose intersection is tail level i's candidate set for
+// candidate l: f(ptr, len, src, pinned) with src = level of the list, or -1 for
+// the shared running list (exploration).  f returns false to stop.
+template <bool STATS, class F>
+__device__ __forceinline__ void for_tail_lists(const DevPlan &P, const WarpState &W, const LeafState &L,
+                                               const Ctx<STATS> &c, const LeafCtx &lc, uint32_t l, uint32_t i, F f) {
+    const uint32_t below = (1u << lc.L0) - 1u;
+    uint32_t shared = P.parents[i] & below, cand = P.parents[i] & ~below;
+    if (lc.explore && shared) {
+        // one running list for the shared parents; a first-parent version is
+        // N(m[j]) itself, pinned when j is a root level
+        const uint32_t lastp = 31 - __clz(shared);
+        if (P.slot[lastp][i] < 0 && lastp < 2 && W.pmode[lastp]) {
+            if (!f(W.lptr[lastp], W.llen[lastp], (int)lastp, true)) return;
+        } else if (!f(version_ptr(P, W, c, lastp, i), W.vlen[lastp][i], -1, false)) {
+            return;
+        }
+        shared = 0;
+    } else if (!lc.explore && P.base[i] >= 0) {
+        // the stored list of an enumerated level (candidatesBefore) replaces its parents
+        const uint32_t bl = (uint32_t)P.base[i];
+        if (bl == 2 && W.pmode[2]) {
+            if (!f(W.flist[bl], W.fcnt[bl], SRC_LEVEL2_LIST, true)) return;
+        } else if (!f(W.flist[bl], W.fcnt[bl], -1, false)) {
+            return;
+        }
+        shared &= P.rest[i];
+        cand &= P.rest[i];
+    }
+    for (uint32_t msk = shared; msk; msk &= msk - 1) {
+        const uint32_t j = __ffs(msk) - 1;
+        if (!f(W.lptr[j], W.llen[j], (int)j, j < 2 && W.pmode[j] != 0)) return;
+    }
+    for (uint32_t msk = cand; msk; msk &= msk - 1) {
+        const uint32_t j = __ffs(msk) - 1;
+        if (!f(L.cptr[l][j - lc.L0], L.clen[l][j - lc.L0], (int)j, false)) return;
+    }
+}
+
+template <bool STATS>
+__device__ __forceinline__ uint32_t tail_list_count(const DevPlan &P, const WarpState &W, const LeafState &L,
+                                                    const Ctx<STATS> &c, const LeafCtx &lc, uint32_t l, uint32_t i) {
+    uint32_t n = 0;
+    for_tail_lists(P, W, L, c, lc, l, i, [&](const uint32_t *, uint32_t, int, bool) { ++n; return true; });
+    return n;
+}
+
+template <bool STATS>
+__device__ __forceinline__ bool in_list(const WarpState &W, const Ctx<STATS> &c, const uint32_t *p, uint32_t len,
+                                        int src, bool pinned, uint32_t y) {
+    if (pinned) {
+        const uint32_t ti = src == SRC_LEVEL2_LIST ? 2u : (uint32_t)src;
+        return pin_has(c.tab + ti * c.tw, W.pmode[ti], c.tw, y);
+    }
+    return contains(p, len, y);
+}
+
+// y ∈ candidates of tail level u for candidate l (bounds, lists, exclusions).
+template <bool STATS>
+__device__ __forceinline__ bool in_tail_set(const DevPlan &P, const WarpState &W, const LeafState &L,
+                                            const Ctx<STATS> &c, const LeafCtx &lc, uint32_t l, uint32_t u,
+                                            uint32_t y) {
+    Bounds b = cand_bounds(P, W, L, lc, l, u);
+    if ((b.has_lo && y <= b.lo) || (b.has_hi && y >= b.hi)) return false;
+    bool ok = true;
+    for_tail_lists(P, W, L, c, lc, l, u, [&](const uint32_t *p, uint32_t len, int src, bool pinned) {
+        ok = in_list(W, c, p, len, src, pinned, y);
+        return ok;
+    });
+    return ok && !cand_excluded(P, W, L, lc, l, u, y);
+}
+
+template <bool STATS>
+__device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32_t L0,
+                                         uint32_t ncand) {
+    LeafState &L = *c.L;
+    const uint32_t lane = lane_id();
+    const uint32_t ne = P.ne, T = P.T;
+    LeafCtx lc{L0, P.join_style == SGE_JOIN_EXPLORATION && L0 > 0};
+    const uint32_t passes = (P.tail_mode == SGE_TAIL_IEP) ? T : 1u;
+    if (P.tail_mode != SGE_TAIL_SINGLE) {
+#pragma unroll
+        for (uint32_t q = 0; q < 16; ++q) L.cnt[lane][q] = 0;
+    }
+    unsigned long long single = 0, bytes = 0;
+    for (uint32_t t = 0; t < passes; ++t) {
+        const uint32_t i = ne + t;
+        // 1. each candidate picks the list it scans (cheapest scan × probes), trimmed by its bounds
+        const uint32_t *bp = nullptr;
+        uint32_t blen = 0;
+        int bsrc = -2;
+        // a tail level with a single list (after reuse) is counted without a
+        // scan: range size minus the matched vertices inside it (numResults)
+        const bool direct = P.tail_mode != SGE_TAIL_IEP && tail_list_count(P, W, L, c, lc, 0, i) == 1;
+        if (direct) {
+            if (lane < ncand) {
+                for_tail_lists(P, W, L, c, lc, lane, i, [&](const uint32_t *p, uint32_t len, int, bool) {
+                    bp = p;
+                    blen = len;
+                    return false;
+                });
+                Bounds b = cand_bounds(P, W, L, lc, lane, i);
+                trim(bp, blen, b);
+                uint32_t cnt = blen;
+                for (uint32_t msk = P.check[i]; msk; msk &= msk - 1) {
+                    const uint32_t v = cand_val(W, L, lc, lane, __ffs(msk) - 1);
+                    if ((!b.has_lo || v > b.lo) && (!b.has_hi || v < b.hi) && contains(bp, blen, v)) --cnt;
+                }
+                if (P.tail_mode == SGE_TAIL_SINGLE) single += cnt;
+                else L.cnt[lane][1] = cnt;
+                if (STATS) bytes += 4ull * (2u + __popc(P.check[i])) * (31u - __clz(blen + 1u));
+            }
+            __syncwarp();
+            continue;
+        }
+        if (lane < ncand) {
+            // scan cost of list q = len(q) × (1 + Σ probe costs of the others)
+            unsigned long long allp = 0, bestcost = ~0ull;
+            for_tail_lists(P, W, L, c, lc, lane, i, [&](const uint32_t *p, uint32_t len, int src, bool pinned) {
+                allp += pinned ? 1u : 2u + (31u - __clz(len + 1u));
+                return true;
+            });
+            for_tail_lists(P, W, L, c, lc, lane, i, [&](const uint32_t *p, uint32_t len, int src, bool pinned) {
+                unsigned long long own = pinned ? 1u : 2u + (31u - __clz(len + 1u));
+                unsigned long long cost = (unsigned long long)len * (allp - own + 1);
+                if (cost < bestcost) { bestcost = cost; bp = p; blen = len; bsrc = src; }
+                if (STATS) bytes += 4ull * len;
+                return true;
+            });
+            Bounds b = cand_bounds(P, W, L, lc, lane, i);
+            trim(bp, blen, b);
+        }
+        L.bptr[lane] = bp;
+        L.blen[lane] = blen;
+        L.bsrc[lane] = bsrc;
+        uint32_t incl = blen;
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            uint32_t v = __shfl_up_sync(FULL_MASK, incl, o);
+            if (lane >= o) incl += v;
+        }
+        L.pref[lane] = incl;
+        const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
+        __syncwarp();
+        // 2. flattened scan: element j belongs to the candidate l with pref[l-1] <= j < pref[l]
+        uint32_t l = 0;
+        const uint32_t nu = (P.tail_mode == SGE_TAIL_IEP) ? (T - 1 - t) : 0u;
+        for (uint32_t j = lane; j < total; j += 32) {
+            while (L.pref[l] <= j) ++l;
+            const uint32_t start = l ? L.pref[l - 1] : 0u;
+            const uint32_t y = L.bptr[l][j - start];
+            const int bs = L.bsrc[l];
+            bool ok = true;
+            for_tail_lists(P, W, L, c, lc, l, i, [&](const uint32_t *p, uint32_t len, int src, bool pinned) {
+                if (src != bs) ok = in_list(W, c, p, len, src, pinned, y);
+                return ok;
+            });
+            if (ok) ok = !cand_excluded(P, W, L, lc, l, i, y);
+            if (!ok) continue;
+            if (P.tail_mode == SGE_TAIL_SINGLE) {
+                ++single;
+            } else if (P.tail_mode == SGE_TAIL_CHOOSE) {
+                atomicAdd(&L.cnt[l][1], 1u);
+            } else {
+                uint32_t fm = 0;
+                for (uint32_t q = 0; q < nu; ++q) fm |= (uint32_t)in_tail_set(P, W, L, c, lc, l, i + 1 + q, y) << q;
+                // every subset s of fm: S[{t} ∪ (s shifted past t)] += 1
+                uint32_t s = fm;
+                while (true) {
+                    atomicAdd(&L.cnt[l][(1u << t) | (s << (t + 1))], 1u);
+                    if (s == 0) break;
+                    s = (s - 1) & fm;
+                }
+            }
+        }
+        __syncwarp();
+    }
+    // 3. per-candidate results
+    unsigned long long r = 0;
+    if (P.tail_mode == SGE_TAIL_SINGLE) {
+        r = single;
+    } else if (lane < ncand) {
+        if (P.tail_mode == SGE_TAIL_CHOOSE) {
+            r = binom_exact(L.cnt[lane][1], T);
+        } else {
+            for (uint32_t p = 0; p < P.nparts; ++p) {
+                unsigned long long term = (unsigned long long)(long long)P.part_coef[p];
+                for (uint32_t bk = 0; bk < P.part_nblocks[p]; ++bk) term *= L.cnt[lane][P.part_block[p][bk]];
+                r += term;
+            }
+        }
+    }
+    if (STATS) {
+        c.alg_bytes += warp_sum_u64(bytes);
+        c.set_ops += (unsigned long long)ncand * passes;
+    }
+    __syncwarp();
+    return warp_sum_u64(r);
+}
+
+// Leaf over up to 32 root edges (plans with only two enumerated levels):
+// lane l < n holds root (u, v).
+template <bool STATS>
+__device__ unsigned long long leaf_roots(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32_t n, uint32_t u,
+                                         uint32_t v) {
+    LeafState &L = *c.L;
+    const uint32_t lane = lane_id();
+    if (lane < n) {
+        L.cm[lane][0] = u;
+        L.cm[lane][1] = v;
+        nbr(c.g, u, L.cptr[lane][0], L.clen[lane][0]);
+        nbr(c.g, v, L.cptr[lane][1], L.clen[lane][1]);
+    }
+    __syncwarp();
+    return leaf_chunk(P, W, c, 0, n);
+}
+
+// One root edge: DFS over levels 2..ne-2; the candidates of level ne-1 go to
+// the leaf 32 at a time.
 template <bool STATS>
 __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32_t u, uint32_t v) {
     const uint32_t lane = lane_id();
-    const bool explore = P.join_style == SGE_JOIN_EXPLORATION;
-    __syncwarp();
-    if (lane == 0) { W.m[0] = u; W.m[1] = v; }
-    __syncwarp();
-    if (explore) {
-        if (!explore_update(P, W, c, 0)) return 0;
-        if (!explore_update(P, W, c, 1)) return 0;
-    }
     const uint32_t ne = P.ne;
-    if (ne == 2) return tail_count(P, W, c);
+    if (ne == 2) return leaf_roots(P, W, c, 1u, u, v);
+    const bool explore = P.join_style == SGE_JOIN_EXPLORATION;
+    const uint32_t L0 = ne - 1;
+    LeafState &L = *c.L;
+    set_match(c.g, W, 0, u);
+    set_match(c.g, W, 1, v);
+    if (P.pin_mask) pin_root(P, W, c);
     unsigned long long acc = 0;
+    bool ok = true;
+    if (explore) ok = explore_update(P, W, c, 0) && explore_update(P, W, c, 1);
     uint32_t lv = 2;
-    if (explore) explore_level(P, W, c, lv);
-    else if (!build_level_wcoj(P, W, c, lv)) return 0;
-    __syncwarp();
-    if (lane == 0) W.pos[lv] = 0;
-    __syncwarp();
-    while (true) {
-        uint32_t pos = W.pos[lv];
+    if (ok) {
+        if (explore) explore_level(P, W, c, lv);
+        else ok = build_level_wcoj(P, W, c, lv);
+        // level 2's list is built once per root; pin it when later levels reuse it
+        if (ok && ((P.pin_mask >> 2) & 1u)) pin_list(W, c, 2, W.flist[2], W.fcnt[2]);
+    }
+    if (ok) {
+        __syncwarp();
+        if (lane == 0) W.pos[lv] = 0;
+        __syncwarp();
+    }
+    while (ok) {
+        if (lv == L0) {
+            const uint32_t n = W.cnt[lv];
+            const uint32_t *lst = W.list[lv];
+            for (uint32_t b0 = 0; b0 < n; b0 += 32) {
+                const uint32_t idx = b0 + lane;
+                bool valid = idx < n;
+                const uint32_t x = valid ? lst[idx] : 0u;
+                if (valid) valid = !excluded(P, W, lv, x);
+                const uint32_t bal = __ballot_sync(FULL_MASK, valid);
+                const uint32_t nc = __popc(bal);
+                if (valid) {
+                    const uint32_t rk = __popc(bal & ((1u << lane) - 1u));
+                    L.cm[rk][0] = x;
+                    nbr(c.g, x, L.cptr[rk][0], L.clen[rk][0]);
+                }
+                __syncwarp();
+                if (nc) acc += leaf_chunk(P, W, c, L0, nc);
+                if (STATS) c.partial += nc;
+            }
+            if (lv == 2) break;
+            --lv;
+            continue;
+        }
+        const uint32_t pos = W.pos[lv];
         if (pos >= W.cnt[lv]) {
             if (lv == 2) break;
             --lv;
             continue;
         }
-        uint32_t x = W.list[lv][pos];
+        const uint32_t x = W.list[lv][pos];
         __syncwarp();
         if (lane == 0) W.pos[lv] = pos + 1;
         __syncwarp();
         if (excluded(P, W, lv, x)) continue;
-        __syncwarp();
-        if (lane == 0) W.m[lv] = x;
-        __syncwarp();
+        set_match(c.g, W, lv, x);
         if (STATS) c.partial += 1;
         if (explore && !explore_update(P, W, c, lv)) continue;
-        if (lv + 1 == ne) {
-            acc += tail_count(P, W, c);
-            continue;
-        }
         ++lv;
         if (explore) explore_level(P, W, c, lv);
-        else if (!build_level_wcoj(P, W, c, lv)) return 0;
+        else if (!build_level_wcoj(P, W, c, lv)) { ok = false; break; }
         __syncwarp();
         if (lane == 0) W.pos[lv] = 0;
         __syncwarp();
     }
-    return acc;
+    if (P.pin_mask) unpin_root(P, W, c);
+    return ok ? acc : 0ull;
+}
+
+// Per-warp shared-memory carve-up: WarpState | LeafState | 3 tables.
+__host__ __device__ constexpr size_t align128(size_t x) { return (x + 127) & ~(size_t)127; }
+__host__ __device__ inline size_t warp_smem_bytes(uint32_t tw) {
+    return align128(sizeof(WarpState)) + align128(sizeof(LeafState)) + align128(3ull * tw * sizeof(uint32_t));
+}
+
+template <bool STATS>
+__device__ __forceinline__ WarpState &setup_warp(unsigned char *smem, uint32_t wib, uint32_t tw, uint32_t tmode,
+                                                 Ctx<STATS> &c) {
+    unsigned char *base = smem + (size_t)wib * warp_smem_bytes(tw);
+    WarpState &W = *reinterpret_cast<WarpState *>(base);
+    c.L = reinterpret_cast<LeafState *>(base + align128(sizeof(WarpState)));
+    c.tab = reinterpret_cast<uint32_t *>(base + align128(sizeof(WarpState)) + align128(sizeof(LeafState)));
+    c.tw = tw;
+    c.tmode = tmode;
+    const uint32_t fill = tmode == 2 ? PIN_EMPTY : 0u;
+    for (uint32_t w = lane_id(); w < 3 * tw; w += 32) c.tab[w] = fill;
+    if (lane_id() == 0) { W.pmode[0] = 0; W.pmode[1] = 0; W.pmode[2] = 0; }
+    __syncwarp();
+    return W;
 }
 
 template <bool STATS>
 __global__ void __launch_bounds__(256) count_kernel(DevGraph g, const DevPlan *__restrict__ plans, uint32_t nplans,
-                                                    unsigned long long total_tasks, unsigned long long *queue,
-                                                    unsigned long long *counts, uint32_t *scratch, uint32_t cap,
-                                                    uint32_t bufs_per_warp, uint32_t chunk,
-                                                    unsigned long long deadline_ns, uint32_t *flags,
-                                                    DevStats *stats) {
-    extern __shared__ unsigned char smem_raw[];
+                                                    unsigned long long *queues, unsigned long long *counts,
+                                                    uint32_t *scratch, uint32_t cap, uint32_t bufs_per_warp,
+                                                    uint32_t tw, uint32_t tmode, unsigned long long deadline_ns,
+                                                    uint32_t *flags, DevStats *stats) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t lane = lane_id();
     const uint32_t wib = threadIdx.x >> 5;
-    WarpState &W = reinterpret_cast<WarpState *>(smem_raw)[wib];
     __shared__ DevPlan Psh[8];
     DevPlan &P = Psh[wib];
     const size_t gwarp = (size_t)blockIdx.x * (blockDim.x >> 5) + wib;
@@ -501,17 +828,24 @@ __global__ void __launch_bounds__(256) count_kernel(DevGraph g, const DevPlan *_
     c.cap = cap;
     c.flags = flags;
     c.set_ops = c.alg_bytes = c.partial = 0;
+    WarpState &W = setup_warp(smem_raw, wib, tw, tmode, c);
     unsigned long long roots = 0;
     unsigned long long tstart = 0;
     if (lane == 0) tstart = globaltimer_ns();
     tstart = __shfl_sync(FULL_MASK, tstart, 0);
-    int cur = -1;
+    // Plans are taken in order; each has its own task queue and chunk size, so
+    // warps spread over the current plan and move on when it is exhausted.
+    uint32_t cur = 0;
     unsigned long long acc = 0;
-    while (true) {
-        unsigned long long t0 = 0;
-        if (lane == 0) t0 = atomicAdd(queue, (unsigned long long)chunk);
-        t0 = __shfl_sync(FULL_MASK, t0, 0);
-        if (t0 >= total_tasks) break;
+    auto load_plan = [&](uint32_t pi) {
+        __syncwarp();
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(plans + pi);
+        uint32_t *dst = reinterpret_cast<uint32_t *>(&P);
+        for (uint32_t w = lane; w < sizeof(DevPlan) / 4; w += 32) dst[w] = src[w];
+        __syncwarp();
+    };
+    if (nplans) load_plan(0);
+    while (cur < nplans) {
         if (deadline_ns) {
             unsigned long long now = 0;
             if (lane == 0) now = globaltimer_ns();
@@ -522,25 +856,39 @@ __global__ void __launch_bounds__(256) count_kernel(DevGraph g, const DevPlan *_
             }
         }
         if (*(volatile uint32_t *)flags & FLAG_OVERFLOW) break;
-        unsigned long long t1 = min(t0 + chunk, total_tasks);
-        for (unsigned long long t = t0; t < t1; ++t) {
-            // locate the plan owning task t (plans are sorted by task_begin)
-            if (cur < 0 || t < P.task_begin || t >= P.task_begin + P.ntasks) {
-                if (cur >= 0 && lane == 0 && acc) atomicAdd(counts + cur, acc);
-                acc = 0;
-                int lo = 0, hi = (int)nplans - 1;
-                while (lo < hi) {
-                    int mid = (lo + hi + 1) >> 1;
-                    if (plans[mid].task_begin <= t) lo = mid; else hi = mid - 1;
+        unsigned long long t0 = 0;
+        if (lane == 0) t0 = atomicAdd(queues + cur, (unsigned long long)P.chunk);
+        t0 = __shfl_sync(FULL_MASK, t0, 0);
+        if (t0 >= P.ntasks) {
+            if (lane == 0 && acc) atomicAdd(counts + cur, acc);
+            acc = 0;
+            if (++cur < nplans) load_plan(cur);
+            continue;
+        }
+        const unsigned long long t1 = min(t0 + P.chunk, P.ntasks);
+        if (P.ne == 2) {
+            // lane l takes task t0 + l
+            const uint32_t n = (uint32_t)(t1 - t0);
+            uint32_t u = 0, v = 0;
+            if (lane < n) {
+                unsigned long long lt = P.root_offset + (t0 + lane) * P.root_stride;
+                uint2 e;
+                if (P.root_kind == SGE_ROOT_ANY) {
+                    e = g.edges[lt >> 1];
+                    if (lt & 1) { uint32_t tmp = e.x; e.x = e.y; e.y = tmp; }
+                } else {
+                    e = g.edges[lt];
+                    if (P.root_kind == SGE_ROOT_DESC) { uint32_t tmp = e.x; e.x = e.y; e.y = tmp; }
                 }
-                cur = lo;
-                __syncwarp();
-                const uint32_t *src = reinterpret_cast<const uint32_t *>(plans + cur);
-                uint32_t *dst = reinterpret_cast<uint32_t *>(&P);
-                for (uint32_t w = lane; w < sizeof(DevPlan) / 4; w += 32) dst[w] = src[w];
-                __syncwarp();
+                u = e.x;
+                v = e.y;
             }
-            unsigned long long lt = P.root_offset + (t - P.task_begin) * P.root_stride;
+            acc += leaf_roots(P, W, c, n, u, v);
+            roots += n;
+            continue;
+        }
+        for (unsigned long long t = t0; t < t1; ++t) {
+            unsigned long long lt = P.root_offset + t * P.root_stride;
             uint2 e;
             if (P.root_kind == SGE_ROOT_ANY) {
                 e = g.edges[lt >> 1];
@@ -553,7 +901,7 @@ __global__ void __launch_bounds__(256) count_kernel(DevGraph g, const DevPlan *_
             ++roots;
         }
     }
-    if (cur >= 0 && lane == 0 && acc) atomicAdd(counts + cur, acc);
+    if (cur < nplans && lane == 0 && acc) atomicAdd(counts + cur, acc);
     if (STATS && lane == 0) {
         atomicAdd(&stats->set_ops, c.set_ops);
         atomicAdd(&stats->alg_bytes, c.alg_bytes);
@@ -648,6 +996,19 @@ void to_devplan(const sge_plan_blob &b, DevPlan &d) {
         nb = b.num_enum;  // stored levels use buffer index = level
     }
     d.nbufs = std::max<uint32_t>(nb, 1);
+    // pin N(m[0]) / N(m[1]) when a level past 2 probes it (probed once per
+    // candidate rather than once per root)
+    d.pin_mask = 0;
+    if (b.num_enum >= 3)
+        for (uint32_t i = 3; i < b.k; ++i) {
+            d.pin_mask |= b.parents[i] & 3u;
+            if (b.join_style == SGE_JOIN_WCOJ && b.base[i] == 2) d.pin_mask |= 4u;
+        }
+    d.keep_full = 0;
+    for (uint32_t i = 0; i < b.k; ++i)
+        if (b.base[i] >= 0) d.keep_full |= 1u << b.base[i];
+    d.mult = b.count_multiplier;
+    d.chunk = 1;
 }
 
 sge_status ensure_scratch(sge_graph *g, size_t bytes) {
@@ -851,9 +1212,16 @@ sge_status sge_count(sge_graph *g, const sge_plan *const *plans, uint32_t nplans
     }
     const uint32_t wpb = o.warps_per_block ? std::min<uint32_t>(o.warps_per_block, 8) : 8;
     const uint32_t threads = wpb * 32;
-    const size_t smem = sizeof(WarpState) * wpb;
+    // pinned-list tables: a bitmap over all vertices when it fits in 4 KB, else a 512-slot hash
+    uint32_t tmode, tw;
+    if (g->n <= 32768u) { tmode = 1; tw = std::max<uint32_t>(32u, ((g->n + 31u) / 32u + 31u) & ~31u); }
+    else { tmode = 2; tw = 512; }
+    const size_t smem = warp_smem_bytes(tw) * wpb;
     const bool want_stats = o.collect_counters != 0;
     int bps = 0;
+    // static (plan copies) + dynamic shared memory exceed the 48 KB default: opt in
+    CUDA_TRY(cudaFuncSetAttribute(count_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CUDA_TRY(cudaFuncSetAttribute(count_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if (want_stats) CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, count_kernel<true>, threads, smem));
     else CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, count_kernel<false>, threads, smem));
     if (o.blocks_per_sm) bps = std::min<int>(bps, (int)o.blocks_per_sm);
@@ -870,23 +1238,26 @@ sge_status sge_count(sge_graph *g, const sge_plan *const *plans, uint32_t nplans
     if (blocks * per_block > budget) blocks = std::max<size_t>(1, budget / std::max<size_t>(per_block, 1));
     sge_status st = ensure_scratch(g, blocks * per_block);
     if (st != SGE_OK) return st;
-    // batch buffer: plans | counts | queue | flags | stats
+    // batch buffer: plans | counts | per-plan queues | flags | stats
     size_t off_plans = 0;
     size_t off_counts = (sizeof(DevPlan) * nplans + 255) & ~(size_t)255;
     size_t off_queue = off_counts + ((8 * (size_t)nplans + 255) & ~(size_t)255);
-    size_t off_flags = off_queue + 256;
+    size_t off_flags = off_queue + ((8 * (size_t)nplans + 255) & ~(size_t)255);
     size_t off_stats = off_flags + 256;
     size_t bytes = off_stats + 256;
     st = ensure_batch(g, bytes);
     if (st != SGE_OK) return st;
     unsigned char *B = g->d_batch;
-    CUDA_TRY(cudaMemcpyAsync(B + off_plans, dps.data(), sizeof(DevPlan) * nplans, cudaMemcpyHostToDevice, g->stream));
     CUDA_TRY(cudaMemsetAsync(B + off_counts, 0, bytes - off_counts, g->stream));
-    uint32_t chunk = o.chunk;
-    if (!chunk) {
-        unsigned long long warps = blocks * wpb;
-        chunk = (uint32_t)std::max<unsigned long long>(1, std::min<unsigned long long>(8, total / (warps * 64 + 1)));
+    {
+        const unsigned long long warps = blocks * wpb;
+        for (auto &d : dps) {
+            if (d.ne == 2) d.chunk = 32;  // one leaf over 32 root edges
+            else if (o.chunk) d.chunk = o.chunk;
+            else d.chunk = (uint32_t)std::max<unsigned long long>(1, std::min<unsigned long long>(8, d.ntasks / (warps * 64 + 1)));
+        }
     }
+    CUDA_TRY(cudaMemcpyAsync(B + off_plans, dps.data(), sizeof(DevPlan) * nplans, cudaMemcpyHostToDevice, g->stream));
     unsigned long long deadline = 0;  // ns after each warp's start; 0 = none
     DevGraph dg{g->d_off, g->d_adj, g->d_edges, g->n, g->m};
     CUDA_TRY(cudaEventRecord(g->ev0, g->stream));
@@ -897,12 +1268,12 @@ sge_status sge_count(sge_graph *g, const sge_plan *const *plans, uint32_t nplans
     DevStats *dstats = reinterpret_cast<DevStats *>(B + off_stats);
     if (o.time_budget_s > 0) deadline = std::max<unsigned long long>(1, (unsigned long long)(o.time_budget_s * 1e9));
     if (want_stats)
-        count_kernel<true><<<(unsigned)blocks, threads, smem, g->stream>>>(dg, dplans, nplans, total, dqueue, dcounts,
-                                                                         g->d_scratch, cap, nbufs, chunk, deadline,
+        count_kernel<true><<<(unsigned)blocks, threads, smem, g->stream>>>(dg, dplans, nplans, dqueue, dcounts,
+                                                                         g->d_scratch, cap, nbufs, tw, tmode, deadline,
                                                                          dflags, dstats);
     else
-        count_kernel<false><<<(unsigned)blocks, threads, smem, g->stream>>>(dg, dplans, nplans, total, dqueue, dcounts,
-                                                                          g->d_scratch, cap, nbufs, chunk, deadline,
+        count_kernel<false><<<(unsigned)blocks, threads, smem, g->stream>>>(dg, dplans, nplans, dqueue, dcounts,
+                                                                          g->d_scratch, cap, nbufs, tw, tmode, deadline,
                                                                           dflags, dstats);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaEventRecord(g->ev1, g->stream));
@@ -980,10 +1351,9 @@ __global__ void __launch_bounds__(256) count_kernel_noalloc(DevGraph g, const De
                                                             unsigned long long *counts, uint32_t *lists,
                                                             uint32_t cap, uint32_t bufs_per_warp, uint32_t chunk,
                                                             uint32_t *flags) {
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t lane = lane_id();
     const uint32_t wib = threadIdx.x >> 5;
-    WarpState &W = reinterpret_cast<WarpState *>(smem_raw)[wib];
     __shared__ DevPlan Psh[8];
     DevPlan &P = Psh[wib];
     const size_t gwarp = (size_t)blockIdx.x * (blockDim.x >> 5) + wib;
@@ -993,6 +1363,7 @@ __global__ void __launch_bounds__(256) count_kernel_noalloc(DevGraph g, const De
     c.cap = cap;
     c.flags = flags;
     c.set_ops = c.alg_bytes = c.partial = 0;
+    WarpState &W = setup_warp(smem_raw, wib, 0u, 0u, c);  // no pinned tables in this variant
     const unsigned long long total = nnz * nplans;
     int cur = -1;
     unsigned long long acc = 0;
@@ -1006,7 +1377,7 @@ __global__ void __launch_bounds__(256) count_kernel_noalloc(DevGraph g, const De
         for (unsigned long long t = t0; t < t1; ++t) {
             const int pi = (int)(t / nnz);
             if (pi != cur) {
-                if (cur >= 0 && lane == 0 && acc) atomicAdd(counts + cur, acc * P.task_begin);
+                if (cur >= 0 && lane == 0 && acc) atomicAdd(counts + cur, acc * P.mult);
                 acc = 0;
                 cur = pi;
                 __syncwarp();
@@ -1023,8 +1394,7 @@ __global__ void __launch_bounds__(256) count_kernel_noalloc(DevGraph g, const De
             acc += run_root<false>(P, W, c, u, v);
         }
     }
-    // P.task_begin carries the plan's count multiplier in this variant
-    if (cur >= 0 && lane == 0 && acc) atomicAdd(counts + cur, acc * P.task_begin);
+    if (cur >= 0 && lane == 0 && acc) atomicAdd(counts + cur, acc * P.mult);
 }
 
 }  // namespace
@@ -1062,7 +1432,7 @@ extern "C" sge_status sge_count_noalloc(const uint32_t *d_offsets, const uint32_
         if (st != SGE_OK) return st;
         DevPlan dp;
         to_devplan(plans[i], dp);
-        dp.task_begin = plans[i].count_multiplier;  // multiplier, applied at the atomic flush
+        dp.task_begin = 0;
         dp.ntasks = nnz;
         dp.root_stride = 1;
         dp.root_offset = 0;
@@ -1074,13 +1444,14 @@ extern "C" sge_status sge_count_noalloc(const uint32_t *d_offsets, const uint32_
     const size_t per_warp = (size_t)nbufs * cap * sizeof(uint32_t);
     const size_t avail = SGE_NOALLOC_SCRATCH_BYTES - NOALLOC_LISTS;
     const uint32_t wpb = 8, threads = wpb * 32;
-    const size_t smem = sizeof(WarpState) * wpb;
+    const size_t smem = warp_smem_bytes(0) * wpb;
     size_t max_blocks = avail / (per_warp * wpb);
     if (max_blocks == 0)
         return fail(SGE_UNSUPPORTED,
                     "sge_count_noalloc: %u levels x max degree %u need %zu bytes per 8-warp block; the static "
                     "scratch holds %zu", nbufs, max_degree, per_warp * wpb, avail);
     int bps = 0, sms = 0;
+    CUDA_TRY(cudaFuncSetAttribute(count_kernel_noalloc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, count_kernel_noalloc, threads, smem));
     CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const size_t blocks = std::max<size_t>(1, std::min<size_t>(max_blocks, (size_t)std::max(bps, 1) * sms));

@@ -307,14 +307,13 @@ bool build_blob(const Pattern &p, const uint32_t *order, const std::vector<std::
         b.rest[i] = b.parents[i];
     }
     // candidate reuse (candidatesBefore): a stored enumerated level l >= 2
-    // whose filters are implied by level i's
+    // whose parents are a subset of level i's (the executor keeps a reused
+    // level's list free of its bounds, so only the parents matter)
     for (uint32_t i = 3; i < k; ++i) {
         int best = -1, best_pc = 0;
         uint32_t lim = std::min(i, ne);
         for (uint32_t l = 2; l < lim; ++l) {
             if ((b.parents[l] & ~b.parents[i]) != 0) continue;
-            if ((b.lower[l] & ~b.lower[i]) != 0) continue;
-            if ((b.upper[l] & ~b.upper[i]) != 0) continue;
             int pc = __builtin_popcount(b.parents[l]);
             if (pc >= 2 && pc >= best_pc) { best = (int)l; best_pc = pc; }
         }
@@ -345,28 +344,34 @@ double plan_cost(const Pattern &p, const sge_plan_blob &b, const Moments &mo) {
         int nb = __builtin_popcount(b.lower[i] | b.upper[i]);
         return std::max(1e-3, L * std::pow(c, r - 1) / std::pow(2.0, nb));
     };
-    auto base_len = [&](uint32_t i) {
-        return b.base[i] >= 0 ? cand[b.base[i]] : L / std::pow(1.0 + c, __builtin_popcount(b.parents[i]) - 1);
+    // lists whose intersection gives level i (a reused stored list counts as one)
+    auto lists = [&](uint32_t i) {
+        return b.base[i] >= 0 ? 1 + __builtin_popcount(b.rest[i]) : __builtin_popcount(b.parents[i]);
     };
-    auto rest_lists = [&](uint32_t i) {
-        return b.base[i] >= 0 ? __builtin_popcount(b.rest[i]) : __builtin_popcount(b.parents[i]) - 1;
-    };
+    auto full_len = [&](uint32_t l) { return std::max(1e-3, L * std::pow(c, __builtin_popcount(b.parents[l]) - 1)); };
+    auto base_len = [&](uint32_t i) { return b.base[i] >= 0 ? std::min(full_len(b.base[i]), L) : L; };
     double N = mo.nnz / ((b.root_kind == SGE_ROOT_ANY) ? 1.0 : 2.0);
     double cost = N * 4.0;
     for (uint32_t i = 2; i < ne; ++i) {
         cand[i] = est_cand(i);
-        double work = (rest_lists(i) > 0 || b.base[i] >= 0) ? base_len(i) * (1.0 + rest_lists(i) * lg) : lg;
+        const double work = lists(i) > 1 ? base_len(i) * (1.0 + (lists(i) - 1) * lg) : lg;
         cost += N * (work + 16.0);
         N *= cand[i];
-        cost += N * 8.0;
+        cost += N * (i + 1 == ne ? 4.0 : 8.0);  // last-level candidates go to the leaf in batches
     }
+    for (uint32_t i = ne; i < k; ++i) cand[i] = est_cand(i);
     double leaf = 0;
-    const uint32_t passes = (b.tail_mode == SGE_TAIL_IEP) ? k - ne : 1u;
-    for (uint32_t t = 0; t < passes; ++t) {
-        uint32_t i = ne + t;
-        double others = 0;
-        for (uint32_t u = i + 1; u < k && b.tail_mode == SGE_TAIL_IEP; ++u) others += __builtin_popcount(b.parents[u]);
-        leaf += base_len(i) * (1.0 + (rest_lists(i) + others) * lg) + 16.0;
+    if (b.tail_mode != SGE_TAIL_IEP && lists(ne) == 1) {
+        // a single list: range size minus matched vertices inside, by binary search
+        leaf = 4.0 + 2.0 * __builtin_popcount(b.check[ne]) * lg;
+    } else {
+        const uint32_t passes = (b.tail_mode == SGE_TAIL_IEP) ? k - ne : 1u;
+        for (uint32_t t = 0; t < passes; ++t) {
+            const uint32_t i = ne + t;
+            double probes = (lists(i) - 1) * lg;
+            for (uint32_t u = i + 1; u < k && b.tail_mode == SGE_TAIL_IEP; ++u) probes += lists(u) * lg;
+            leaf += base_len(i) * (1.0 + probes) + 4.0;
+        }
     }
     cost += N * leaf;
     return cost;
@@ -538,7 +543,7 @@ sge_status sge_plan_validate(const sge_plan_blob *b) {
         if (b->base[i] >= 0) {
             uint32_t l = (uint32_t)b->base[i];
             if (l < 2 || l >= i || l >= ne) return fail(SGE_BAD_INPUT, "level %u reuses level %u", i, l);
-            if ((b->parents[l] & ~b->parents[i]) || (b->lower[l] & ~b->lower[i]) || (b->upper[l] & ~b->upper[i]))
+            if (b->parents[l] & ~b->parents[i])
                 return fail(SGE_BAD_INPUT, "level %u reuse of level %u is not implied", i, l);
             if ((b->parents[l] | b->rest[i]) != b->parents[i]) return fail(SGE_BAD_INPUT, "level %u rest mask inconsistent", i);
         } else if (b->base[i] != -1) {
