@@ -63,6 +63,8 @@ struct DevPlan {
     uint32_t chunk;                               // root tasks per queue grab
     uint32_t pin_mask;                            // levels 0/1 whose lists are pinned in shared memory
     uint32_t keep_full;                           // levels whose bound-free list later levels reuse
+    uint32_t hoist_mask;                          // tail levels whose list is computed early (WCOJ)
+    uint32_t hoist_at[SGE_MAX_K];                 // level after whose match a hoisted list is computed
 };
 
 struct DevStats {
@@ -84,6 +86,7 @@ struct WarpState {
     uint32_t llen[SGE_MAX_K];
     uint32_t vlen[SGE_MAX_K][SGE_MAX_K];  // exploration version lengths (j, i)
     uint32_t pmode[3];                    // pinned N(m[0]), N(m[1]), level-2 list: 0 none, 1 bitmap, 2 hash
+    uint32_t hcnt[SGE_MAX_K];             // hoisted tail lists (buffer slot = level)
 };
 
 // Leaf state (shared memory): up to 32 candidates of the last enumerated
@@ -323,7 +326,7 @@ __device__ __forceinline__ void wcoj_base(const DevPlan &P, const WarpState &W, 
 // Warp-cooperative filter of [bp, bp+blen) by membership in all parent lists
 // of `rest` and by the exclusion set of level i; stores the survivors (in
 // order) to out when STORE.  Returns the survivor count (warp-uniform).
-template <bool STATS, bool STORE>
+template <bool STATS, bool STORE, bool EXCLUDE = true>
 __device__ __forceinline__ uint32_t setop(const DevPlan &P, const WarpState &W, Ctx<STATS> &c, uint32_t i,
                                           const uint32_t *bp, uint32_t blen, uint32_t rest, uint32_t *out) {
     const uint32_t lane = lane_id();
@@ -338,7 +341,7 @@ __device__ __forceinline__ uint32_t setop(const DevPlan &P, const WarpState &W, 
         bool ok = idx < blen;
         uint32_t x = ok ? bp[idx] : 0u;
         for (uint32_t msk = rest; msk && ok; msk &= msk - 1) ok = in_level_list(W, c, __ffs(msk) - 1, x);
-        if (ok) ok = !excluded(P, W, i, x);
+        if (EXCLUDE && ok) ok = !excluded(P, W, i, x);
         uint32_t bal = __ballot_sync(FULL_MASK, ok);
         if (STORE) {
             uint32_t p = total + __popc(bal & ((1u << lane) - 1u));
@@ -379,6 +382,49 @@ __device__ __forceinline__ bool build_level_wcoj(const DevPlan &P, WarpState &W,
     __syncwarp();
     if (lane_id() == 0) { W.flist[i] = fp; W.fcnt[i] = fl; W.list[i] = ip; W.cnt[i] = il; }
     __syncwarp();
+    return true;
+}
+
+// Hoisting: a tail level whose parents are all matched before the last
+// enumerated level gets its full intersection computed once, right after its
+// last parent is matched (bounds and exclusions are applied at the leaf).
+template <bool STATS>
+__device__ __forceinline__ bool hoist_after(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32_t j) {
+    for (uint32_t msk = P.hoist_mask; msk; msk &= msk - 1) {
+        const uint32_t i = __ffs(msk) - 1;
+        if (P.hoist_at[i] != j) continue;
+        const uint32_t *bp;
+        uint32_t blen, rest;
+        if (P.base[i] >= 0 && (uint32_t)P.base[i] <= j) {
+            // a reused level's full list (built when that level was entered)
+            bp = W.flist[P.base[i]];
+            blen = W.fcnt[P.base[i]];
+            rest = P.rest[i];
+        } else {
+            uint32_t best = 0;
+            unsigned long long bestcost = ~0ull;
+            for (uint32_t pm = P.parents[i]; pm; pm &= pm - 1) {
+                const uint32_t q = __ffs(pm) - 1;
+                unsigned long long probes = 0;
+                for (uint32_t o = P.parents[i] & ~(1u << q); o; o &= o - 1)
+                    probes += probe_cost(W, __ffs(o) - 1, W.llen[__ffs(o) - 1]);
+                const unsigned long long cost = (unsigned long long)W.llen[q] * (probes + 1);
+                if (cost < bestcost) { bestcost = cost; best = q; }
+            }
+            bp = W.lptr[best];
+            blen = W.llen[best];
+            rest = P.parents[i] & ~(1u << best);
+        }
+        uint32_t *out = c.buf + (size_t)i * c.cap;
+        const uint32_t n = setop<STATS, true, false>(P, W, c, i, bp, blen, rest, out);
+        __syncwarp();
+        if (lane_id() == 0) W.hcnt[i] = n;
+        __syncwarp();
+        if (n > c.cap) {
+            if (lane_id() == 0) atomicOr(c.flags, FLAG_OVERFLOW);
+            return false;
+        }
+    }
     return true;
 }
 
@@ -464,6 +510,7 @@ __device__ __forceinline__ void explore_level(const DevPlan &P, WarpState &W, Ct
 // List identity used by the leaf for the pinned stored list of level 2
 // (distinct from the level numbers that name CSR lists).
 constexpr int SRC_LEVEL2_LIST = 40;
+constexpr int SRC_HOISTED = 41;
 
 struct LeafCtx {
     uint32_t L0;
@@ -502,6 +549,10 @@ __device__ __forceinline__ void for_tail_lists(const DevPlan &P, const WarpState
                                                const Ctx<STATS> &c, const LeafCtx &lc, uint32_t l, uint32_t i, F f) {
     const uint32_t below = (1u << lc.L0) - 1u;
     uint32_t shared = P.parents[i] & below, cand = P.parents[i] & ~below;
+    if (!lc.explore && ((P.hoist_mask >> i) & 1u)) {
+        f(c.buf + (size_t)i * c.cap, W.hcnt[i], SRC_HOISTED, false);
+        return;
+    }
     if (lc.explore && shared) {
         // one running list for the shared parents; a first-parent version is
         // N(m[j]) itself, pinned when j is a root level
@@ -727,6 +778,7 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
     unsigned long long acc = 0;
     bool ok = true;
     if (explore) ok = explore_update(P, W, c, 0) && explore_update(P, W, c, 1);
+    else if (P.hoist_mask) ok = hoist_after(P, W, c, 1);
     uint32_t lv = 2;
     if (ok) {
         if (explore) explore_level(P, W, c, lv);
@@ -777,6 +829,7 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
         set_match(c.g, W, lv, x);
         if (STATS) c.partial += 1;
         if (explore && !explore_update(P, W, c, lv)) continue;
+        if (!explore && P.hoist_mask && !hoist_after(P, W, c, lv)) { ok = false; break; }
         ++lv;
         if (explore) explore_level(P, W, c, lv);
         else if (!build_level_wcoj(P, W, c, lv)) { ok = false; break; }
@@ -993,7 +1046,7 @@ void to_devplan(const sge_plan_blob &b, DevPlan &d) {
             }
         }
     } else {
-        nb = b.num_enum;  // stored levels use buffer index = level
+        nb = b.k;  // stored levels and hoisted tail lists use buffer index = level
     }
     d.nbufs = std::max<uint32_t>(nb, 1);
     // pin N(m[0]) / N(m[1]) when a level past 2 probes it (probed once per
@@ -1007,6 +1060,17 @@ void to_devplan(const sge_plan_blob &b, DevPlan &d) {
     d.keep_full = 0;
     for (uint32_t i = 0; i < b.k; ++i)
         if (b.base[i] >= 0) d.keep_full |= 1u << b.base[i];
+    // hoist tail levels with >= 2 parents that are all matched before the last enumerated level
+    d.hoist_mask = 0;
+    if (b.join_style == SGE_JOIN_WCOJ && b.num_enum >= 3)
+        for (uint32_t i = b.num_enum; i < b.k; ++i) {
+            const uint32_t par = b.parents[i];
+            const uint32_t last = 31u - (uint32_t)__builtin_clz(par);
+            if (__builtin_popcount(par) >= 2 && last + 1 < b.num_enum) {
+                d.hoist_mask |= 1u << i;
+                d.hoist_at[i] = last < 1 ? 1u : last;
+            }
+        }
     d.mult = b.count_multiplier;
     d.chunk = 1;
 }

@@ -312,6 +312,10 @@ bool build_blob(const Pattern &p, const uint32_t *order, const std::vector<std::
     for (uint32_t i = 3; i < k; ++i) {
         int best = -1, best_pc = 0;
         uint32_t lim = std::min(i, ne);
+        // a tail level whose parents all precede the last enumerated level is
+        // computed right after its last parent (hoisted): reuse only levels built by then
+        const uint32_t lastp = 31u - (uint32_t)__builtin_clz(b.parents[i]);
+        if (i >= ne && __builtin_popcount(b.parents[i]) >= 2 && lastp + 1 < ne) lim = std::min(lim, std::max(lastp, 1u) + 1);
         for (uint32_t l = 2; l < lim; ++l) {
             if ((b.parents[l] & ~b.parents[i]) != 0) continue;
             int pc = __builtin_popcount(b.parents[l]);
@@ -352,25 +356,48 @@ double plan_cost(const Pattern &p, const sge_plan_blob &b, const Moments &mo) {
     auto base_len = [&](uint32_t i) { return b.base[i] >= 0 ? std::min(full_len(b.base[i]), L) : L; };
     double N = mo.nnz / ((b.root_kind == SGE_ROOT_ANY) ? 1.0 : 2.0);
     double cost = N * 4.0;
+    double Nat[SGE_MAX_K];
+    Nat[1] = N;
     for (uint32_t i = 2; i < ne; ++i) {
         cand[i] = est_cand(i);
         const double work = lists(i) > 1 ? base_len(i) * (1.0 + (lists(i) - 1) * lg) : lg;
         cost += N * (work + 16.0);
         N *= cand[i];
+        Nat[i] = N;
         cost += N * (i + 1 == ne ? 4.0 : 8.0);  // last-level candidates go to the leaf in batches
     }
+    for (uint32_t i = ne; i < k; ++i) {
+        const uint32_t par = b.parents[i];
+        const uint32_t last = 31u - (uint32_t)__builtin_clz(par);
+        if (__builtin_popcount(par) >= 2 && last + 1 < ne) {
+            const bool reuse = b.base[i] >= 0 && (uint32_t)b.base[i] <= std::max(last, 1u);
+            const double work = reuse ? base_len(i) * (1.0 + __builtin_popcount(b.rest[i]) * lg)
+                                      : L * (1.0 + (__builtin_popcount(par) - 1) * lg);
+            cost += Nat[std::max(last, 1u)] * (work + 16.0);
+        }
+    }
     for (uint32_t i = ne; i < k; ++i) cand[i] = est_cand(i);
+    // a tail level whose parents precede the last enumerated level is hoisted:
+    // its intersection is computed once per match of its last parent
+    // (WCOJ), or is the running list (exploration) — one list at the leaf
+    auto hoisted = [&](uint32_t i) {
+        const uint32_t par = b.parents[i];
+        return __builtin_popcount(par) >= 2 && (31u - (uint32_t)__builtin_clz(par)) + 1 < ne;
+    };
+    auto leaf_lists = [&](uint32_t i) { return hoisted(i) ? 1 : lists(i); };
     double leaf = 0;
-    if (b.tail_mode != SGE_TAIL_IEP && lists(ne) == 1) {
+    if (b.tail_mode != SGE_TAIL_IEP && leaf_lists(ne) == 1) {
         // a single list: range size minus matched vertices inside, by binary search
         leaf = 4.0 + 2.0 * __builtin_popcount(b.check[ne]) * lg;
     } else {
         const uint32_t passes = (b.tail_mode == SGE_TAIL_IEP) ? k - ne : 1u;
         for (uint32_t t = 0; t < passes; ++t) {
             const uint32_t i = ne + t;
-            double probes = (lists(i) - 1) * lg;
-            for (uint32_t u = i + 1; u < k && b.tail_mode == SGE_TAIL_IEP; ++u) probes += lists(u) * lg;
-            leaf += base_len(i) * (1.0 + probes) + 4.0;
+            double probes = (leaf_lists(i) - 1) * lg;
+            for (uint32_t u = i + 1; u < k && b.tail_mode == SGE_TAIL_IEP; ++u) probes += leaf_lists(u) * lg;
+            const double bl = hoisted(i) ? std::max(1e-3, L * std::pow(c, __builtin_popcount(b.parents[i]) - 1))
+                                         : base_len(i);
+            leaf += bl * (1.0 + probes) + 4.0;
         }
     }
     cost += N * leaf;
