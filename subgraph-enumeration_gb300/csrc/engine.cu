@@ -64,6 +64,10 @@ struct DevPlan {
     uint32_t pin_mask;                            // levels 0/1 whose lists are pinned in shared memory
     uint32_t keep_full;                           // levels whose bound-free list later levels reuse
     uint32_t hoist_mask;                          // tail levels whose list is computed early (WCOJ)
+    uint32_t split_par;                           // level 2's parents (levels 0/1): bounds its list by degree
+    uint32_t split_H;                             // roots whose level-2 bound exceeds this are deferred
+    uint32_t split_S;                             // level-2 candidates per deferred task (0 = never defer)
+    uint32_t split_C;                             // deferred tasks per heavy root (max degree / S, rounded up)
     uint32_t hoist_at[SGE_MAX_K];                 // level after whose match a hoisted list is computed
 };
 
@@ -196,6 +200,7 @@ struct Ctx {
     uint32_t tw;
     uint32_t tmode;   // 0 none, 1 bitmap over all vertices, 2 open-addressing hash
     LeafState *L;
+    unsigned long long tstart, deadline;  // globaltimer of the warp's start; budget in ns (0 = none)
     unsigned long long set_ops, alg_bytes, partial;
 };
 
@@ -764,8 +769,23 @@ __device__ unsigned long long leaf_roots(const DevPlan &P, WarpState &W, Ctx<STA
 
 // One root edge: DFS over levels 2..ne-2; the candidates of level ne-1 go to
 // the leaf 32 at a time.
+// Past the time budget?  (all lanes agree: lane 0 reads the clock)
 template <bool STATS>
-__device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32_t u, uint32_t v) {
+__device__ __forceinline__ bool out_of_time(Ctx<STATS> &c) {
+    if (!c.deadline) return false;
+    unsigned long long now = 0;
+    if (lane_id() == 0) now = globaltimer_ns();
+    now = __shfl_sync(FULL_MASK, now, 0);
+    if (now - c.tstart <= c.deadline) return false;
+    if (lane_id() == 0) atomicOr(c.flags, FLAG_TIMEOUT);
+    return true;
+}
+
+// r2b/r2e restrict the level-2 candidates processed (a heavy root is split
+// into several tasks over ranges of its level-2 list).
+template <bool STATS>
+__device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32_t u, uint32_t v,
+                                       uint32_t r2b = 0u, uint32_t r2e = 0xFFFFFFFFu) {
     const uint32_t lane = lane_id();
     const uint32_t ne = P.ne;
     if (ne == 2) return leaf_roots(P, W, c, 1u, u, v);
@@ -788,14 +808,18 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
     }
     if (ok) {
         __syncwarp();
-        if (lane == 0) W.pos[lv] = 0;
+        if (lane == 0) {
+            W.cnt[2] = min(W.cnt[2], r2e);
+            W.pos[2] = min(r2b, W.cnt[2]);
+        }
         __syncwarp();
     }
     while (ok) {
         if (lv == L0) {
             const uint32_t n = W.cnt[lv];
             const uint32_t *lst = W.list[lv];
-            for (uint32_t b0 = 0; b0 < n; b0 += 32) {
+            for (uint32_t b0 = W.pos[lv]; b0 < n; b0 += 32) {
+                if (out_of_time(c)) { ok = false; break; }
                 const uint32_t idx = b0 + lane;
                 bool valid = idx < n;
                 const uint32_t x = valid ? lst[idx] : 0u;
@@ -821,6 +845,7 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
             --lv;
             continue;
         }
+        if (out_of_time(c)) { ok = false; break; }
         const uint32_t x = W.list[lv][pos];
         __syncwarp();
         if (lane == 0) W.pos[lv] = pos + 1;
@@ -863,12 +888,40 @@ __device__ __forceinline__ WarpState &setup_warp(unsigned char *smem, uint32_t w
     return W;
 }
 
+// Root task t of plan P -> directed root edge (u, v).
+__device__ __forceinline__ uint2 root_edge(const DevGraph &g, const DevPlan &P, unsigned long long t) {
+    const unsigned long long lt = P.root_offset + t * P.root_stride;
+    uint2 e;
+    if (P.root_kind == SGE_ROOT_ANY) {
+        e = g.edges[lt >> 1];
+        if (lt & 1) { uint32_t tmp = e.x; e.x = e.y; e.y = tmp; }
+    } else {
+        e = g.edges[lt];
+        if (P.root_kind == SGE_ROOT_DESC) { uint32_t tmp = e.x; e.x = e.y; e.y = tmp; }
+    }
+    return e;
+}
+
+// Upper bound on a root's level-2 list: the smaller degree among level 2's
+// root parents.
+__device__ __forceinline__ uint32_t level2_bound(const DevGraph &g, const DevPlan &P, uint2 e) {
+    uint32_t ub = 0xFFFFFFFFu;
+    if (P.split_par & 1u) ub = min(ub, __ldg(g.off + e.x + 1) - __ldg(g.off + e.x));
+    if (P.split_par & 2u) ub = min(ub, __ldg(g.off + e.y + 1) - __ldg(g.off + e.y));
+    return ub;
+}
+
+// Phase 0 counts every root, except that a root whose level-2 bound exceeds
+// split_H is appended to its plan's heavy list (while there is room) instead.
+// Phase 1 runs the heavy roots as split_C tasks each, task c covering level-2
+// candidates [c·S, (c+1)·S); tasks past a root's bound end at once.
 template <bool STATS>
-__global__ void __launch_bounds__(256) count_kernel(DevGraph g, const DevPlan *__restrict__ plans, uint32_t nplans,
+__global__ void __launch_bounds__(256, 3) count_kernel(DevGraph g, const DevPlan *__restrict__ plans, uint32_t nplans,
                                                     unsigned long long *queues, unsigned long long *counts,
                                                     uint32_t *scratch, uint32_t cap, uint32_t bufs_per_warp,
                                                     uint32_t tw, uint32_t tmode, unsigned long long deadline_ns,
-                                                    uint32_t *flags, DevStats *stats) {
+                                                    uint32_t *flags, DevStats *stats, uint32_t phase,
+                                                    uint32_t *heavy_cnt, uint32_t *heavy_ids, uint32_t heavy_cap) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t lane = lane_id();
     const uint32_t wib = threadIdx.x >> 5;
@@ -885,54 +938,48 @@ __global__ void __launch_bounds__(256) count_kernel(DevGraph g, const DevPlan *_
     unsigned long long roots = 0;
     unsigned long long tstart = 0;
     if (lane == 0) tstart = globaltimer_ns();
-    tstart = __shfl_sync(FULL_MASK, tstart, 0);
+    c.tstart = __shfl_sync(FULL_MASK, tstart, 0);
+    c.deadline = deadline_ns;
     // Plans are taken in order; each has its own task queue and chunk size, so
     // warps spread over the current plan and move on when it is exhausted.
     uint32_t cur = 0;
-    unsigned long long acc = 0;
+    unsigned long long acc = 0, ntasks = 0;
     auto load_plan = [&](uint32_t pi) {
         __syncwarp();
         const uint32_t *src = reinterpret_cast<const uint32_t *>(plans + pi);
         uint32_t *dst = reinterpret_cast<uint32_t *>(&P);
         for (uint32_t w = lane; w < sizeof(DevPlan) / 4; w += 32) dst[w] = src[w];
         __syncwarp();
+        ntasks = phase == 0 ? P.ntasks : (unsigned long long)min(heavy_cnt[pi], heavy_cap) * P.split_C;
     };
     if (nplans) load_plan(0);
     while (cur < nplans) {
-        if (deadline_ns) {
-            unsigned long long now = 0;
-            if (lane == 0) now = globaltimer_ns();
-            now = __shfl_sync(FULL_MASK, now, 0);
-            if (now - tstart > deadline_ns) {
-                if (lane == 0) atomicOr(flags, FLAG_TIMEOUT);
-                break;
-            }
-        }
+        if (out_of_time(c)) break;
         if (*(volatile uint32_t *)flags & FLAG_OVERFLOW) break;
+        const uint32_t chunk = phase == 0 ? P.chunk : 1u;
         unsigned long long t0 = 0;
-        if (lane == 0) t0 = atomicAdd(queues + cur, (unsigned long long)P.chunk);
+        if (lane == 0) t0 = atomicAdd(queues + cur, (unsigned long long)chunk);
         t0 = __shfl_sync(FULL_MASK, t0, 0);
-        if (t0 >= P.ntasks) {
+        if (t0 >= ntasks) {
             if (lane == 0 && acc) atomicAdd(counts + cur, acc);
             acc = 0;
             if (++cur < nplans) load_plan(cur);
             continue;
         }
-        const unsigned long long t1 = min(t0 + P.chunk, P.ntasks);
+        const unsigned long long t1 = min(t0 + chunk, ntasks);
+        if (phase == 1) {
+            const uint32_t h = (uint32_t)(t0 / P.split_C), part = (uint32_t)(t0 % P.split_C);
+            const uint2 e = root_edge(g, P, heavy_ids[(size_t)cur * heavy_cap + h]);
+            if ((unsigned long long)part * P.split_S < level2_bound(g, P, e))
+                acc += run_root<STATS>(P, W, c, e.x, e.y, part * P.split_S, (part + 1) * P.split_S);
+            continue;
+        }
         if (P.ne == 2) {
             // lane l takes task t0 + l
             const uint32_t n = (uint32_t)(t1 - t0);
             uint32_t u = 0, v = 0;
             if (lane < n) {
-                unsigned long long lt = P.root_offset + (t0 + lane) * P.root_stride;
-                uint2 e;
-                if (P.root_kind == SGE_ROOT_ANY) {
-                    e = g.edges[lt >> 1];
-                    if (lt & 1) { uint32_t tmp = e.x; e.x = e.y; e.y = tmp; }
-                } else {
-                    e = g.edges[lt];
-                    if (P.root_kind == SGE_ROOT_DESC) { uint32_t tmp = e.x; e.x = e.y; e.y = tmp; }
-                }
+                const uint2 e = root_edge(g, P, t0 + lane);
                 u = e.x;
                 v = e.y;
             }
@@ -941,17 +988,18 @@ __global__ void __launch_bounds__(256) count_kernel(DevGraph g, const DevPlan *_
             continue;
         }
         for (unsigned long long t = t0; t < t1; ++t) {
-            unsigned long long lt = P.root_offset + t * P.root_stride;
-            uint2 e;
-            if (P.root_kind == SGE_ROOT_ANY) {
-                e = g.edges[lt >> 1];
-                if (lt & 1) { uint32_t tmp = e.x; e.x = e.y; e.y = tmp; }
-            } else {
-                e = g.edges[lt];
-                if (P.root_kind == SGE_ROOT_DESC) { uint32_t tmp = e.x; e.x = e.y; e.y = tmp; }
+            const uint2 e = root_edge(g, P, t);
+            ++roots;
+            if (P.split_S && level2_bound(g, P, e) > P.split_H) {
+                uint32_t slot = 0;
+                if (lane == 0) slot = atomicAdd(heavy_cnt + cur, 1u);
+                slot = __shfl_sync(FULL_MASK, slot, 0);
+                if (slot < heavy_cap) {
+                    if (lane == 0) heavy_ids[(size_t)cur * heavy_cap + slot] = (uint32_t)t;
+                    continue;
+                }
             }
             acc += run_root<STATS>(P, W, c, e.x, e.y);
-            ++roots;
         }
     }
     if (cur < nplans && lane == 0 && acc) atomicAdd(counts + cur, acc);
@@ -1073,6 +1121,8 @@ void to_devplan(const sge_plan_blob &b, DevPlan &d) {
         }
     d.mult = b.count_multiplier;
     d.chunk = 1;
+    d.split_par = b.num_enum >= 3 ? (b.parents[2] & 3u) : 0u;
+    d.split_S = 0;  // set per graph in sge_count
 }
 
 sge_status ensure_scratch(sge_graph *g, size_t bytes) {
@@ -1302,17 +1352,35 @@ sge_status sge_count(sge_graph *g, const sge_plan *const *plans, uint32_t nplans
     if (blocks * per_block > budget) blocks = std::max<size_t>(1, budget / std::max<size_t>(per_block, 1));
     sge_status st = ensure_scratch(g, blocks * per_block);
     if (st != SGE_OK) return st;
-    // batch buffer: plans | counts | per-plan queues | flags | stats
+    // heavy-root splitting (plans with >= 3 enumerated levels): roots whose
+    // level-2 list may exceed 4·S candidates run as tasks of S candidates
+    const uint32_t split_S = 128, split_H = 4 * split_S;
+    bool any_split = false;
+    unsigned long long max_tasks = 1;
+    for (auto &d : dps) {
+        if (d.ne >= 3 && g->max_deg > split_H) {
+            d.split_S = split_S;
+            d.split_H = split_H;
+            d.split_C = (g->max_deg + split_S - 1) / split_S;
+            any_split = true;
+        }
+        max_tasks = std::max(max_tasks, d.ntasks);
+    }
+    const uint32_t heavy_cap = any_split ? (uint32_t)std::min<unsigned long long>(max_tasks, 1ull << 20) : 1u;
+    // batch buffer: plans | counts | per-plan queues | flags | stats | heavy counts | heavy lists
     size_t off_plans = 0;
     size_t off_counts = (sizeof(DevPlan) * nplans + 255) & ~(size_t)255;
     size_t off_queue = off_counts + ((8 * (size_t)nplans + 255) & ~(size_t)255);
     size_t off_flags = off_queue + ((8 * (size_t)nplans + 255) & ~(size_t)255);
     size_t off_stats = off_flags + 256;
-    size_t bytes = off_stats + 256;
+    size_t off_hcnt = off_stats + 256;
+    size_t off_hids = off_hcnt + ((4 * (size_t)nplans + 255) & ~(size_t)255);
+    size_t bytes_zeroed = off_hids;
+    size_t bytes = off_hids + (((size_t)heavy_cap * nplans * 4 + 255) & ~(size_t)255);
     st = ensure_batch(g, bytes);
     if (st != SGE_OK) return st;
     unsigned char *B = g->d_batch;
-    CUDA_TRY(cudaMemsetAsync(B + off_counts, 0, bytes - off_counts, g->stream));
+    CUDA_TRY(cudaMemsetAsync(B + off_counts, 0, bytes_zeroed - off_counts, g->stream));
     {
         const unsigned long long warps = blocks * wpb;
         for (auto &d : dps) {
@@ -1330,16 +1398,23 @@ sge_status sge_count(sge_graph *g, const sge_plan *const *plans, uint32_t nplans
     unsigned long long *dqueue = reinterpret_cast<unsigned long long *>(B + off_queue);
     uint32_t *dflags = reinterpret_cast<uint32_t *>(B + off_flags);
     DevStats *dstats = reinterpret_cast<DevStats *>(B + off_stats);
+    uint32_t *dhcnt = reinterpret_cast<uint32_t *>(B + off_hcnt);
+    uint32_t *dhids = reinterpret_cast<uint32_t *>(B + off_hids);
     if (o.time_budget_s > 0) deadline = std::max<unsigned long long>(1, (unsigned long long)(o.time_budget_s * 1e9));
-    if (want_stats)
-        count_kernel<true><<<(unsigned)blocks, threads, smem, g->stream>>>(dg, dplans, nplans, dqueue, dcounts,
-                                                                         g->d_scratch, cap, nbufs, tw, tmode, deadline,
-                                                                         dflags, dstats);
-    else
-        count_kernel<false><<<(unsigned)blocks, threads, smem, g->stream>>>(dg, dplans, nplans, dqueue, dcounts,
-                                                                          g->d_scratch, cap, nbufs, tw, tmode, deadline,
-                                                                          dflags, dstats);
-    CUDA_TRY(cudaGetLastError());
+    uint32_t launches = 0;
+    for (uint32_t phase = 0; phase < (any_split ? 2u : 1u); ++phase) {
+        if (phase == 1) CUDA_TRY(cudaMemsetAsync(dqueue, 0, 8 * (size_t)nplans, g->stream));
+        if (want_stats)
+            count_kernel<true><<<(unsigned)blocks, threads, smem, g->stream>>>(
+                dg, dplans, nplans, dqueue, dcounts, g->d_scratch, cap, nbufs, tw, tmode, deadline, dflags, dstats,
+                phase, dhcnt, dhids, heavy_cap);
+        else
+            count_kernel<false><<<(unsigned)blocks, threads, smem, g->stream>>>(
+                dg, dplans, nplans, dqueue, dcounts, g->d_scratch, cap, nbufs, tw, tmode, deadline, dflags, dstats,
+                phase, dhcnt, dhids, heavy_cap);
+        CUDA_TRY(cudaGetLastError());
+        ++launches;
+    }
     CUDA_TRY(cudaEventRecord(g->ev1, g->stream));
     std::vector<unsigned long long> hc(nplans);
     uint32_t hflags = 0;
@@ -1361,7 +1436,7 @@ sge_status sge_count(sge_graph *g, const sge_plan *const *plans, uint32_t nplans
         stats->set_ops = hs.set_ops;
         stats->alg_bytes = hs.alg_bytes;
         stats->partial_matches = hs.partial;
-        stats->gpu_launches = 1;
+        stats->gpu_launches = launches;
         stats->status_flags = hflags;
         stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
     }
@@ -1428,6 +1503,8 @@ __global__ void __launch_bounds__(256) count_kernel_noalloc(DevGraph g, const De
     c.flags = flags;
     c.set_ops = c.alg_bytes = c.partial = 0;
     WarpState &W = setup_warp(smem_raw, wib, 0u, 0u, c);  // no pinned tables in this variant
+    c.tstart = 0;
+    c.deadline = 0;
     const unsigned long long total = nnz * nplans;
     int cur = -1;
     unsigned long long acc = 0;
