@@ -233,6 +233,36 @@ sge_status sge_plan_pattern_stats(uint32_t k, uint32_t m, const uint32_t *edges,
 /* |Aut(P)| and whether the reference would run a single-bag plan. */
 sge_status sge_pattern_info(uint32_t k, uint32_t m, const uint32_t *edges,
                             uint64_t *aut_size, uint32_t *single_bag);
+/* Every executable plan of the pattern, cheapest first by the cost model
+ * (at most cap; the chosen plan of sge_plan_pattern_stats is element 0). */
+sge_status sge_plan_candidates(uint32_t k, uint32_t m, const uint32_t *edges, const sge_graph_stats *stats,
+                               const sge_plan_opts *opts, sge_plan_blob *out, uint32_t cap, uint32_t *n_out);
+/* Fixed-length feature vector of a plan for the learned scorer. */
+#define SGE_FEATURES 64u
+sge_status sge_plan_features(const sge_plan_blob *blob, const sge_graph_stats *stats, float *out);
+
+/* ---- learned plan scorer (the cost slot of optCostOrder, plan/optimizer.cpp:441-577) ----
+ * A 3-layer MLP (in → hidden → hidden → 1, ReLU) predicting a plan's log
+ * runtime.  Trained on the GPU in FP32 (Adam, MSE); batched inference in BF16
+ * on the tensor cores.  Parameters are one flat FP32 array: W1[h×in], b1[h],
+ * W2[h×h], b2[h], W3[h], b3[1]. */
+typedef struct sge_mlp sge_mlp;
+sge_status sge_mlp_create(uint32_t in_dim, uint32_t hidden, uint64_t seed, int device, sge_mlp **out);
+sge_status sge_mlp_destroy(sge_mlp *m);
+sge_status sge_mlp_num_params(const sge_mlp *m, size_t *n);
+sge_status sge_mlp_get_params(const sge_mlp *m, float *out);
+sge_status sge_mlp_set_params(sge_mlp *m, const float *in);
+sge_status sge_mlp_forward(sge_mlp *m, const float *x, uint32_t batch, float *y);       /* FP32 */
+sge_status sge_mlp_forward_bf16(sge_mlp *m, const float *x, uint32_t batch, float *y);  /* BF16 tensor cores */
+sge_status sge_mlp_loss_grad(sge_mlp *m, const float *x, const float *t, uint32_t batch, float *loss, float *grads);
+sge_status sge_mlp_train(sge_mlp *m, const float *x, const float *t, uint32_t n, uint32_t epochs, uint32_t batch,
+                         float lr, uint64_t seed, float *final_loss);
+/* Plans with the learned scorer: the cost model's best `shortlist` candidates
+ * are scored by the MLP (BF16) and the lowest predicted runtime wins. */
+sge_status sge_plan_pattern_learned(uint32_t k, uint32_t m, const uint32_t *edges, const sge_graph_stats *stats,
+                                    const sge_plan_opts *opts, sge_mlp *scorer, uint32_t shortlist,
+                                    sge_plan_blob *out);
+
 /* Check a plan blob for internal consistency (levels, masks, tail validity). */
 sge_status sge_plan_validate(const sge_plan_blob *blob);
 

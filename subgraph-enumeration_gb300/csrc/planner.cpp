@@ -27,6 +27,7 @@
 #include <array>
 #include <cmath>
 #include <cstring>
+#include <cstddef>
 #include <vector>
 
 using namespace sge;
@@ -442,9 +443,10 @@ sge_status sge_plan_pattern(uint32_t k, uint32_t m, const uint32_t *edges, const
     return sge_plan_pattern_stats(k, m, edges, nullptr, opts, out);
 }
 
-sge_status sge_plan_pattern_stats(uint32_t k, uint32_t m, const uint32_t *edges, const sge_graph_stats *gs,
-                                  const sge_plan_opts *opts, sge_plan_blob *out) {
-    if (!out) return fail(SGE_BAD_INPUT, "sge_plan_pattern: null output");
+// Collects every valid plan of the pattern with its cost-model estimate,
+// cheapest first, without duplicates.
+static sge_status collect_candidates(uint32_t k, uint32_t m, const uint32_t *edges, const sge_graph_stats *gs,
+                                     const sge_plan_opts *opts, std::vector<Candidate> &out) {
     Pattern p;
     sge_status st = make_pattern(k, m, edges, p);
     if (st != SGE_OK) return st;
@@ -471,8 +473,7 @@ sge_status sge_plan_pattern_stats(uint32_t k, uint32_t m, const uint32_t *edges,
         mo.nnz = 16e6;
         for (uint32_t d = 0; d < SGE_MAX_K + 2; ++d) mo.M[d] = 1e6 * std::pow(16.0, (double)d);
     }
-    bool have_best = false;
-    Candidate best{};
+    out.clear();
     auto consider = [&](const uint32_t *order) {
         // two restriction schemes: stabilize in matching order, or in reverse
         for (int scheme = 0; scheme < 2; ++scheme) {
@@ -485,7 +486,7 @@ sge_status sge_plan_pattern_stats(uint32_t k, uint32_t m, const uint32_t *edges,
                 if (!build_blob(p, order, restr, T, o.use_iep != 0, o.join_style, aut.size(), single, c.blob)) continue;
                 c.cost = plan_cost(p, c.blob, mo);
                 c.blob.est_cost = c.cost;
-                if (!have_best || c.cost < best.cost * (1 - 1e-12)) { best = c; have_best = true; }
+                out.push_back(c);
             }
         }
     };
@@ -496,7 +497,7 @@ sge_status sge_plan_pattern_stats(uint32_t k, uint32_t m, const uint32_t *edges,
             seen |= 1u << o.force_order[i];
         }
         consider(o.force_order);
-        if (!have_best) return fail(SGE_BAD_INPUT, "force_order is not a connected order starting with an edge");
+        if (out.empty()) return fail(SGE_BAD_INPUT, "force_order is not a connected order starting with an edge");
     } else if (k <= 8) {
         uint32_t order[SGE_MAX_K];
         for (uint32_t i = 0; i < k; ++i) order[i] = i;
@@ -511,8 +512,8 @@ sge_status sge_plan_pattern_stats(uint32_t k, uint32_t m, const uint32_t *edges,
             if (conn) consider(order);
         } while (next_perm(order, k));
     } else {
-        // greedy: start from the highest-degree edge, add the vertex with the
-        // most edges into the matched set (ties: higher pattern degree)
+        // greedy: start from each edge, add the vertex with the most edges into
+        // the matched set (ties: higher pattern degree)
         for (uint32_t a = 0; a < k; ++a)
             for (uint32_t bb = 0; bb < k; ++bb) {
                 if (!p.edge(a, bb)) continue;
@@ -524,8 +525,8 @@ sge_status sge_plan_pattern_stats(uint32_t k, uint32_t m, const uint32_t *edges,
                     int bestv = -1, bs = -1;
                     for (uint32_t v = 0; v < k; ++v) {
                         if ((seen >> v) & 1u) continue;
-                        int s = __builtin_popcount(p.adj[v] & seen) * 64 + p.deg(v);
-                        if (__builtin_popcount(p.adj[v] & seen) > 0 && s > bs) { bs = s; bestv = (int)v; }
+                        int sc = __builtin_popcount(p.adj[v] & seen) * 64 + p.deg(v);
+                        if (__builtin_popcount(p.adj[v] & seen) > 0 && sc > bs) { bs = sc; bestv = (int)v; }
                     }
                     order[i] = (uint32_t)bestv;
                     seen |= 1u << bestv;
@@ -533,8 +534,80 @@ sge_status sge_plan_pattern_stats(uint32_t k, uint32_t m, const uint32_t *edges,
                 consider(order);
             }
     }
-    if (!have_best) return fail(SGE_UNSUPPORTED, "no executable plan found for the pattern");
-    *out = best.blob;
+    if (out.empty()) return fail(SGE_UNSUPPORTED, "no executable plan found for the pattern");
+    std::stable_sort(out.begin(), out.end(), [](const Candidate &x, const Candidate &y) { return x.cost < y.cost; });
+    // drop exact duplicates (same blob up to the cost field)
+    std::vector<Candidate> uniq;
+    for (auto &c : out) {
+        bool dup = false;
+        for (auto &u : uniq)
+            if (u.blob.k == c.blob.k && memcmp(&u.blob, &c.blob, offsetof(sge_plan_blob, est_cost)) == 0) { dup = true; break; }
+        if (!dup) uniq.push_back(c);
+        if (uniq.size() >= 4096) break;
+    }
+    out.swap(uniq);
+    return SGE_OK;
+}
+
+sge_status sge_plan_pattern_stats(uint32_t k, uint32_t m, const uint32_t *edges, const sge_graph_stats *gs,
+                                  const sge_plan_opts *opts, sge_plan_blob *out) {
+    if (!out) return fail(SGE_BAD_INPUT, "sge_plan_pattern: null output");
+    std::vector<Candidate> cands;
+    sge_status st = collect_candidates(k, m, edges, gs, opts, cands);
+    if (st != SGE_OK) return st;
+    *out = cands.front().blob;
+    return SGE_OK;
+}
+
+sge_status sge_plan_candidates(uint32_t k, uint32_t m, const uint32_t *edges, const sge_graph_stats *gs,
+                               const sge_plan_opts *opts, sge_plan_blob *out, uint32_t cap, uint32_t *n_out) {
+    if (!out || !n_out || cap == 0) return fail(SGE_BAD_INPUT, "sge_plan_candidates: bad argument");
+    std::vector<Candidate> cands;
+    sge_status st = collect_candidates(k, m, edges, gs, opts, cands);
+    if (st != SGE_OK) return st;
+    uint32_t n = (uint32_t)std::min<size_t>(cap, cands.size());
+    for (uint32_t i = 0; i < n; ++i) out[i] = cands[i].blob;
+    *n_out = n;
+    return SGE_OK;
+}
+
+sge_status sge_plan_features(const sge_plan_blob *b, const sge_graph_stats *gs, float *f) {
+    if (!b || !f) return fail(SGE_BAD_INPUT, "sge_plan_features: null argument");
+    for (uint32_t i = 0; i < SGE_FEATURES; ++i) f[i] = 0.f;
+    auto lg2 = [](double x) { return (float)std::log2(x + 1.0); };
+    if (gs) {
+        f[0] = lg2(gs->num_vertices) / 32.f;
+        f[1] = lg2(gs->num_directed_edges) / 32.f;
+        f[2] = lg2(gs->moments[2] / std::max(gs->moments[1], 1.0)) / 16.f;
+        f[3] = (float)gs->clustering;
+        f[4] = lg2(gs->max_degree) / 24.f;
+    }
+    uint32_t medges = 0, tailpar = 0;
+    for (uint32_t i = 0; i < b->k; ++i) medges += __builtin_popcount(b->parents[i]);
+    for (uint32_t i = b->num_enum; i < b->k; ++i) tailpar += __builtin_popcount(b->parents[i]);
+    f[5] = b->k / 16.f;
+    f[6] = b->k > 1 ? (float)medges / (b->k * (b->k - 1) / 2) : 0.f;
+    f[7] = lg2((double)b->aut_size) / 16.f;
+    f[8] = b->num_enum / 16.f;
+    f[9] = b->tail_len / 4.f;
+    if (b->tail_mode >= 1 && b->tail_mode <= 3) f[9 + b->tail_mode] = 1.f;  // 10..12
+    f[13] = (float)b->join_style;
+    if (b->root_kind <= 2) f[14 + b->root_kind] = 1.f;  // 14..16
+    f[17] = b->num_restrictions / 16.f;
+    f[18] = (float)b->single_bag;
+    f[19] = lg2(b->est_cost) / 64.f;
+    for (uint32_t l = 2; l < 9 && l < b->k; ++l) {
+        float *q = f + 20 + (l - 2) * 6;
+        const uint32_t last = b->parents[l] ? 31u - (uint32_t)__builtin_clz(b->parents[l]) : 0u;
+        q[0] = __builtin_popcount(b->parents[l]) / 8.f;
+        q[1] = __builtin_popcount(b->lower[l] | b->upper[l]) / 4.f;
+        q[2] = b->base[l] >= 0 ? 1.f : 0.f;
+        q[3] = __builtin_popcount(b->rest[l]) / 8.f;
+        q[4] = l >= b->num_enum ? 1.f : 0.f;
+        q[5] = (l >= b->num_enum && __builtin_popcount(b->parents[l]) >= 2 && last + 1 < b->num_enum) ? 1.f : 0.f;
+    }
+    f[62] = tailpar / 16.f;
+    f[63] = 1.f;
     return SGE_OK;
 }
 
@@ -595,3 +668,22 @@ sge_status sge_plan_validate(const sge_plan_blob *b) {
 }
 
 }  // extern "C"
+
+extern "C" sge_status sge_plan_pattern_learned(uint32_t k, uint32_t m, const uint32_t *edges,
+                                               const sge_graph_stats *gs, const sge_plan_opts *opts, sge_mlp *scorer,
+                                               uint32_t shortlist, sge_plan_blob *out) {
+    if (!out || !scorer) return fail(SGE_BAD_INPUT, "sge_plan_pattern_learned: null argument");
+    std::vector<Candidate> cands;
+    sge_status st = collect_candidates(k, m, edges, gs, opts, cands);
+    if (st != SGE_OK) return st;
+    const uint32_t n = (uint32_t)std::min<size_t>(shortlist ? shortlist : 64u, cands.size());
+    std::vector<float> feats((size_t)n * SGE_FEATURES), pred(n);
+    for (uint32_t i = 0; i < n; ++i) sge_plan_features(&cands[i].blob, gs, &feats[(size_t)i * SGE_FEATURES]);
+    st = sge_mlp_forward_bf16(scorer, feats.data(), n, pred.data());
+    if (st != SGE_OK) return st;
+    uint32_t best = 0;
+    for (uint32_t i = 1; i < n; ++i)
+        if (pred[i] < pred[best]) best = i;
+    *out = cands[best].blob;
+    return SGE_OK;
+}

@@ -128,6 +128,20 @@ SIGNATURES = {
     "sge_plan_destroy": (C.c_int, [C.c_void_p]),
     "sge_count": (C.c_int, [C.c_void_p, _P(C.c_void_p), u32, _P(CountOpts), _P(u64), _P(u64), _P(Stats)]),
     "sge_count_host": (C.c_int, [_P(u32), _P(u32), u32, u64, _P(PlanBlob), u32, _P(CountOpts), _P(u64), _P(Stats)]),
+    "sge_plan_candidates": (C.c_int, [u32, u32, _P(u32), _P(GraphStats), _P(PlanOpts), _P(PlanBlob), u32, _P(u32)]),
+    "sge_plan_features": (C.c_int, [_P(PlanBlob), _P(GraphStats), _P(C.c_float)]),
+    "sge_mlp_create": (C.c_int, [u32, u32, u64, C.c_int, _P(C.c_void_p)]),
+    "sge_mlp_destroy": (C.c_int, [C.c_void_p]),
+    "sge_mlp_num_params": (C.c_int, [C.c_void_p, _P(C.c_size_t)]),
+    "sge_mlp_get_params": (C.c_int, [C.c_void_p, _P(C.c_float)]),
+    "sge_mlp_set_params": (C.c_int, [C.c_void_p, _P(C.c_float)]),
+    "sge_mlp_forward": (C.c_int, [C.c_void_p, _P(C.c_float), u32, _P(C.c_float)]),
+    "sge_mlp_forward_bf16": (C.c_int, [C.c_void_p, _P(C.c_float), u32, _P(C.c_float)]),
+    "sge_mlp_loss_grad": (C.c_int, [C.c_void_p, _P(C.c_float), _P(C.c_float), u32, _P(C.c_float), _P(C.c_float)]),
+    "sge_mlp_train": (C.c_int, [C.c_void_p, _P(C.c_float), _P(C.c_float), u32, u32, u32, C.c_float, u64,
+                                _P(C.c_float)]),
+    "sge_plan_pattern_learned": (C.c_int, [u32, u32, _P(u32), _P(GraphStats), _P(PlanOpts), C.c_void_p, u32,
+                                           _P(PlanBlob)]),
     "sge_count_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, u32, u64, u32, _P(PlanBlob), u32, C.c_void_p,
                                     C.c_void_p]),
 }
@@ -307,6 +321,107 @@ def plan(pattern: PatternGraph, graph: "Engine | GraphStats | DataGraph | None" 
     else:
         _check(lib().sge_plan_pattern(pattern.k, pattern.m, _u32p(e), graph._h if graph else None, C.byref(o),
                                       C.byref(b)))
+    return b
+
+
+SGE_FEATURES = 64
+
+
+def _plan_opts(iep: bool, exploration: bool, max_tail: int, seed: int) -> PlanOpts:
+    return PlanOpts(JOIN_EXPLORATION if exploration else JOIN_WCOJ, int(iep), max_tail, seed, None)
+
+
+def candidates(pattern: PatternGraph, stats: "GraphStats | None", iep: bool = True, exploration: bool = False,
+               cap: int = 64, max_tail: int = SGE_MAX_TAIL) -> list[PlanBlob]:
+    """Every executable plan of the pattern, cheapest first by the cost model."""
+    arr = (PlanBlob * cap)()
+    n = u32()
+    e = pattern.flat()
+    o = _plan_opts(iep, exploration, max_tail, 1)
+    _check(lib().sge_plan_candidates(pattern.k, pattern.m, _u32p(e), C.byref(stats) if stats is not None else None,
+                                     C.byref(o), arr, cap, C.byref(n)))
+    return [PlanBlob.from_buffer_copy(arr[i]) for i in range(n.value)]
+
+
+def features(blob: PlanBlob, stats: "GraphStats | None") -> np.ndarray:
+    out = np.zeros(SGE_FEATURES, np.float32)
+    _check(lib().sge_plan_features(C.byref(blob), C.byref(stats) if stats is not None else None,
+                                   out.ctypes.data_as(C.POINTER(C.c_float))))
+    return out
+
+
+def _fp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class MLP:
+    """The learned plan scorer (sge_mlp): FP32 training and BF16 inference on the GPU."""
+
+    def __init__(self, in_dim: int = SGE_FEATURES, hidden: int = 128, seed: int = 0, device: int = 0):
+        h = C.c_void_p()
+        _check(lib().sge_mlp_create(in_dim, hidden, seed, device, C.byref(h)))
+        self._h = h
+        self.in_dim, self.hidden = in_dim, hidden
+
+    @property
+    def num_params(self) -> int:
+        n = C.c_size_t()
+        _check(lib().sge_mlp_num_params(self._h, C.byref(n)))
+        return n.value
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.num_params, np.float32)
+        _check(lib().sge_mlp_get_params(self._h, _fp(out)))
+        return out
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.num_params
+        _check(lib().sge_mlp_set_params(self._h, _fp(p)))
+
+    def forward(self, x: np.ndarray, bf16: bool = False) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.zeros(x.shape[0], np.float32)
+        fn = lib().sge_mlp_forward_bf16 if bf16 else lib().sge_mlp_forward
+        _check(fn(self._h, _fp(x), x.shape[0], _fp(y)))
+        return y
+
+    def loss_grad(self, x: np.ndarray, t: np.ndarray) -> tuple[float, np.ndarray]:
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        loss = C.c_float()
+        g = np.zeros(self.num_params, np.float32)
+        _check(lib().sge_mlp_loss_grad(self._h, _fp(x), _fp(t), x.shape[0], C.byref(loss), _fp(g)))
+        return float(loss.value), g
+
+    def train(self, x: np.ndarray, t: np.ndarray, epochs: int = 200, batch: int = 256, lr: float = 1e-3,
+              seed: int = 0) -> float:
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        loss = C.c_float()
+        _check(lib().sge_mlp_train(self._h, _fp(x), _fp(t), x.shape[0], epochs, batch, lr, seed, C.byref(loss)))
+        return float(loss.value)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().sge_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def plan_learned(pattern: PatternGraph, stats: "GraphStats", scorer: MLP, iep: bool = True,
+                 exploration: bool = False, shortlist: int = 64) -> PlanBlob:
+    """Plans with the learned scorer (cost-model shortlist, MLP picks)."""
+    b = PlanBlob()
+    e = pattern.flat()
+    o = _plan_opts(iep, exploration, SGE_MAX_TAIL, 1)
+    _check(lib().sge_plan_pattern_learned(pattern.k, pattern.m, _u32p(e), C.byref(stats), C.byref(o), scorer._h,
+                                          shortlist, C.byref(b)))
     return b
 
 

@@ -1,0 +1,77 @@
+"""Records the learned scorer's training data on a GPU and trains the shipped
+weights.
+
+  python tests/golden/make_plan_runtimes.py OUT_DIR
+
+For seeded synthetic patterns (7-vertex, 16-19 edges, and 6-vertex, 11-13
+edges; seeds disjoint from every benchmark batch) on seeded R-MAT graphs
+(a=.57 b=.19 c=.19; scale 9 with 4,000 edges and scale 10 with 8,000 edges),
+the cost model's 8-plan shortlist of each pattern is run over all root edges
+and the kernel time recorded (sge_learn.record); every candidate of a pattern
+must give the same count.  A candidate past 0.5 s is recorded as censored.
+Recording stops after a wall-clock budget (argument 2, seconds).  Writes OUT_DIR/plan_runtimes.npz (the
+fixture tests/golden/plan_runtimes.npz) and OUT_DIR/mlp_weights.npz (the
+scorer checkpoint subgraph-enumeration_gb300/scorer/mlp_weights.npz), trained
+on the patterns marked for training only.
+"""
+import json
+import sys
+import time
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(REPO / "subgraph-enumeration_gb300"))
+import numpy as np  # noqa: E402
+
+import sge  # noqa: E402
+import sge_learn  # noqa: E402
+
+
+def main(out: Path, budget_s: float):
+    out.mkdir(parents=True, exist_ok=True)
+    graphs = {"rmat_s9": sge.gen_rmat(9, 4000, seed=5), "rmat_s10": sge.gen_rmat(10, 8000, seed=5)}
+    rec = sge_learn.Records()
+    meta = {"graphs": {}, "patterns": []}
+    pid = 0
+    t0 = time.time()
+    for gname, g in graphs.items():
+        st = g.stats()
+        meta["graphs"][gname] = g.fingerprint()
+        pats = []
+        for i in range(24):
+            pats.append(("6v", sge.PatternGraph.random(6, 11 + i % 3, 8000 + i)))
+            pats.append(("7v", sge.PatternGraph.random(7, 16 + i % 4, 9000 + i)))
+        with sge.Engine(g) as eng:
+            for kind, p in pats:
+                if time.time() - t0 > budget_s * (0.5 if gname == "rmat_s9" else 1.0):
+                    break
+                n0 = len(rec.count)
+                sge_learn.record(eng, st, [p], shortlist=8, stride=1, pattern_offset=pid, time_budget_s=0.5, rec=rec)
+                done = [c for c, ms in zip(rec.count[n0:], rec.ms[n0:]) if ms < 1000.0]
+                assert len(set(done)) <= 1, f"candidate plans disagree: {done}"
+                meta["patterns"].append({"id": pid, "graph": gname, "kind": kind, "k": p.k,
+                                         "edges": p.edges.tolist(), "train": pid % 4 != 3})
+                pid += 1
+                print(f"{gname} {kind} pattern {pid} recorded ({time.time() - t0:.0f}s)", flush=True)
+    rec.save(out / "plan_runtimes.npz")
+    (out / "plan_runtimes.json").write_text(json.dumps(meta))
+    # shipped weights: trained on the training patterns only
+    p, c, x, ms, cnt = rec.arrays()
+    train_ids = {m["id"] for m in meta["patterns"] if m["train"]}
+    tr = sge_learn.Records()
+    for i in range(len(p)):
+        if int(p[i]) in train_ids:
+            tr.pattern.append(int(p[i])); tr.cand.append(int(c[i])); tr.x.append(x[i].tolist())
+            tr.ms.append(float(ms[i])); tr.count.append(int(cnt[i]))
+    mlp = sge_learn.train(tr, epochs=400, seed=0)
+    sge_learn.save_mlp(mlp, out / "mlp_weights.npz")
+    te = sge_learn.Records()
+    for i in range(len(p)):
+        if int(p[i]) not in train_ids:
+            te.pattern.append(int(p[i])); te.cand.append(int(c[i])); te.x.append(x[i].tolist())
+            te.ms.append(float(ms[i])); te.count.append(int(cnt[i]))
+    print("held-out regret", sge_learn.regret(te, mlp), flush=True)
+
+
+if __name__ == "__main__":
+    main(Path(sys.argv[1]), float(sys.argv[2]) if len(sys.argv) > 2 else 300.0)
