@@ -228,9 +228,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plans", default="", help="comma-separated subset, e.g. house/wcoj-u (profiling)")
     ap.add_argument("--per-plan", action="store_true", help="time each plan alone and print one JSON per plan")
+    ap.add_argument("--workload", default="chunglu7100", choices=["chunglu7100", "batch7"],
+                    help="batch7: 78 random 7-vertex patterns, learned+batched vs plain planning (separate line)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch7":
+        return run_batch7(args)
     world, rank, local = dist_env()
     import torch
     import sge
@@ -272,19 +276,23 @@ def main():
     # algorithmic bytes of one launch (stats variant, untimed)
     _, _, st = eng.count(plans, stats=True, **shard)
     alg_bytes = st["alg_bytes"]
-    # timed steps: flush L2 before each, time each launch on its own stream
-    kernel_ms, host_ms, counts = [], [], None
+    # timed steps: one replay of the captured batch (CUDA graph) per step, L2
+    # flushed before each; device time from events around the graph launch
+    kernel_ms, host_ms, counts, launches = [], [], None, 0
+    batch = eng.batch(plans, **shard)
     with ClockSampler(device) as clk:
         for _ in range(args.steps):
             flush.fill_(1)
             barrier()
             t0 = time.perf_counter()
-            c, inst, s = eng.count(plans, stats=False, **shard)
+            c, inst, s = batch.run()
             t1 = time.perf_counter()
             barrier()
             kernel_ms.append(s["kernel_ms"])
             host_ms.append((t1 - t0) * 1e3)
+            launches += s["gpu_launches"]
             counts = c
+    batch.close()
     # reduce over ranks: counts summed, times max
     if dist:
         tc = torch.tensor(counts, dtype=torch.int64, device=f"cuda:{device}")
@@ -327,7 +335,7 @@ def main():
                              "CSR offset pair; the CSR is L2-resident at this size"},
         "e2e": {"value": e2e_value, "unit": "embeddings/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": statistics.median(e2e_ms)},
-        "gpu_launches": args.steps,
+        "gpu_launches": launches,
         "clocks": clk.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -337,6 +345,84 @@ def main():
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+BATCH7_GRAPH = dict(scale=10, m=8000, a=0.57, b=0.19, c=0.19, seed=4)
+
+
+def run_batch7(args):
+    """Learned + batched vs plain planning on a batch of 78 seeded random
+    7-vertex patterns (16-19 edges) over a seeded R-MAT graph (scale 10,
+    8,000 edges: the batch configuration's generator at a size whose exact
+    counts finish in seconds).  Wall time includes planning.
+      plain:   per pattern, cost-model plan then its own launch (as the
+               reference runs one process per pattern)
+      learned: shortlists on host threads, one BF16 MLP scoring call for all
+               patterns, one launch of all plans replayed from a CUDA graph."""
+    import concurrent.futures as cf
+    import numpy as np
+    import torch
+    import sge
+    import sge_learn
+    gs = BATCH7_GRAPH
+    g = sge.gen_rmat(gs["scale"], gs["m"], gs["a"], gs["b"], gs["c"], gs["seed"])
+    pats = [sge.PatternGraph.random(7, 16 + i % 4, 2000 + i) for i in range(78)]
+    eng = sge.Engine(g)
+    st = g.stats()
+    mlp = sge_learn.load_mlp()
+
+    def plain():
+        t0 = time.perf_counter()
+        counts, plan_s, kern = [], 0.0, 0.0
+        for p in pats:
+            a = time.perf_counter()
+            b = sge.plan(p, st)
+            plan_s += time.perf_counter() - a
+            c, _, s = eng.count([b])
+            kern += s["kernel_ms"]
+            counts.append(c[0])
+        return counts, time.perf_counter() - t0, plan_s, kern
+
+    def learned():
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+            shortlists = list(ex.map(lambda p: sge.candidates(p, st, cap=64), pats))
+        feats = np.concatenate([np.stack([sge.features(b, st) for b in sl]) for sl in shortlists])
+        pred = mlp.forward(feats, bf16=True)
+        plans, o = [], 0
+        for sl in shortlists:
+            plans.append(sl[int(np.argmin(pred[o:o + len(sl)]))])
+            o += len(sl)
+        plan_s = time.perf_counter() - t0
+        with eng.batch(plans) as bt:
+            c, _, s = bt.run()
+        return c, time.perf_counter() - t0, plan_s, s["kernel_ms"]
+
+    for _ in range(args.warmup):
+        learned()
+    pw, lw, pk, lk, pp, lp = [], [], [], [], [], []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        cp, tp, plan_p, kp = plain()
+        cl, tl, plan_l, kl = learned()
+        assert cp == cl, "plain and learned plans disagree"
+        pw.append(tp); lw.append(tl); pk.append(kp); lk.append(kl); pp.append(plan_p); lp.append(plan_l)
+    total = sum(cl)
+    line = {"metric": "embeddings/sec, learned+batched planning and execution (wall time incl. planning)",
+            "value": total / statistics.median(lw), "unit": "embeddings/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(lw), "higher_is_better": True,
+            "scaling": "strong", "vs_baseline": None, "dtype": "u32 ids / u64 counts", "data": "synthetic",
+            "config": {"workload": "rmat_s10_m8000 x 78 random 7-vertex patterns (16-19 edges)",
+                       "graph": dict(gs, generator="rmat"), "patterns": "PatternGraph.random(7, 16 + i%4, 2000 + i)"},
+            "learned_batched": {"wall_s": statistics.median(lw), "planning_s": statistics.median(lp),
+                                "kernel_ms": statistics.median(lk)},
+            "plain": {"wall_s": statistics.median(pw), "planning_s": statistics.median(pp),
+                      "kernel_ms": statistics.median(pk), "value": total / statistics.median(pw)},
+            "speedup_wall": statistics.median(pw) / statistics.median(lw),
+            "speedup_kernel": statistics.median(pk) / statistics.median(lk),
+            "total_count": total}
+    eng.close()
+    print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

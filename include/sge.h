@@ -284,6 +284,15 @@ sge_status sge_plan_destroy(sge_plan *p);
 sge_status sge_count(sge_graph *g, const sge_plan *const *plans, uint32_t nplans,
                      const sge_count_opts *opts, uint64_t *counts, uint64_t *instances,
                      sge_stats *stats);
+/* A batch prepared once and replayed from a captured CUDA graph: the plans
+ * are uploaded and the launch sequence (counter reset, both launch phases,
+ * read-back of counts, flags and counters) is captured at creation; each run
+ * is one graph launch.  The batch owns its device buffers; g must outlive it. */
+typedef struct sge_batch sge_batch;
+sge_status sge_batch_create(sge_graph *g, const sge_plan *const *plans, uint32_t nplans, const sge_count_opts *opts,
+                            sge_batch **out);
+sge_status sge_batch_run(sge_batch *b, uint64_t *counts, uint64_t *instances, sge_stats *stats);
+sge_status sge_batch_destroy(sge_batch *b);
 /* End-to-end convenience: host CSR in, counts out (H2D copy, count, D2H read
  * and release all inside the call). */
 sge_status sge_count_host(const uint32_t *offsets, const uint32_t *nbrs, uint32_t num_vertices,

@@ -1202,6 +1202,154 @@ double sample_clustering(const uint32_t *off, const uint32_t *nb, uint32_t n) {
 }
 }  // namespace sge
 
+namespace {
+// Everything one counting launch needs, computed on the host.
+struct LaunchCfg {
+    std::vector<DevPlan> dps;
+    uint32_t nplans = 0, wpb = 8, threads = 256, tmode = 0, tw = 0, cap = 0, nbufs = 1, heavy_cap = 1;
+    size_t smem = 0, blocks = 1, scratch_bytes = 0;
+    bool want_stats = false, any_split = false;
+    unsigned long long deadline = 0;
+    size_t off_plans = 0, off_counts = 0, off_queue = 0, off_flags = 0, off_stats = 0, off_hcnt = 0, off_hids = 0,
+           bytes_zeroed = 0, bytes = 0;
+};
+
+sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t nplans, const sge_count_opts &o,
+                          size_t scratch_held, LaunchCfg &L) {
+    L.nplans = nplans;
+    L.dps.resize(nplans);
+    unsigned long long total = 0;
+    for (uint32_t i = 0; i < nplans; ++i) {
+        if (!plans[i]) return fail(SGE_BAD_INPUT, "plan %u is null", i);
+        DevPlan &d = L.dps[i];
+        d = plans[i]->dp;
+        d.task_begin = total;
+        const unsigned long long all = (d.root_kind == SGE_ROOT_ANY) ? 2ull * g->m : g->m;
+        const unsigned long long stride = o.root_stride > 1 ? o.root_stride : 1ull;
+        const unsigned long long offs = o.root_offset;
+        if (stride > 1 && offs >= stride) return fail(SGE_BAD_INPUT, "root_offset %llu >= root_stride %llu", offs, stride);
+        d.root_stride = stride;
+        d.root_offset = stride > 1 ? offs : 0;
+        d.ntasks = all > d.root_offset ? (all - d.root_offset + stride - 1) / stride : 0;
+        total += d.ntasks;
+        L.nbufs = std::max(L.nbufs, d.nbufs);
+        if (d.k > SGE_MAX_K) return fail(SGE_UNSUPPORTED, "plan %u has k=%u", i, d.k);
+    }
+    L.wpb = o.warps_per_block ? std::min<uint32_t>(o.warps_per_block, 8) : 8;
+    L.threads = L.wpb * 32;
+    // pinned-list tables: a bitmap over all vertices when it fits in 4 KB, else a 512-slot hash
+    if (g->n <= 32768u) { L.tmode = 1; L.tw = std::max<uint32_t>(32u, ((g->n + 31u) / 32u + 31u) & ~31u); }
+    else { L.tmode = 2; L.tw = 512; }
+    L.smem = warp_smem_bytes(L.tw) * L.wpb;
+    L.want_stats = o.collect_counters != 0;
+    int bps = 0;
+    // static (plan copies) + dynamic shared memory exceed the 48 KB default: opt in
+    CUDA_TRY(cudaFuncSetAttribute(count_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
+    CUDA_TRY(cudaFuncSetAttribute(count_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
+    if (L.want_stats) CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, count_kernel<true>, L.threads, L.smem));
+    else CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, count_kernel<false>, L.threads, L.smem));
+    if (o.blocks_per_sm) bps = std::min<int>(bps, (int)o.blocks_per_sm);
+    bps = std::max(bps, 1);
+    L.cap = o.max_level_capacity ? o.max_level_capacity : std::max<uint32_t>(g->max_deg, 1);
+    L.cap = (L.cap + 31) & ~31u;
+    // fit the scratch into a quarter of free memory by trimming resident blocks
+    size_t free_b = 0, tot_b = 0;
+    CUDA_TRY(cudaMemGetInfo(&free_b, &tot_b));
+    const size_t per_block = (size_t)L.wpb * L.nbufs * L.cap * sizeof(uint32_t);
+    size_t blocks = (size_t)g->num_sms * bps;
+    const size_t budget = free_b / 4 + scratch_held;
+    while (blocks > (size_t)g->num_sms && blocks * per_block > budget) blocks -= g->num_sms;
+    if (blocks * per_block > budget) blocks = std::max<size_t>(1, budget / std::max<size_t>(per_block, 1));
+    L.blocks = blocks;
+    L.scratch_bytes = blocks * per_block;
+    // heavy-root splitting (plans with >= 3 enumerated levels): roots whose
+    // level-2 list may exceed 4·S candidates run as tasks of S candidates
+    const uint32_t split_S = 128, split_H = 4 * split_S;
+    unsigned long long max_tasks = 1;
+    const unsigned long long warps = blocks * L.wpb;
+    for (auto &d : L.dps) {
+        if (d.ne >= 3 && g->max_deg > split_H) {
+            d.split_S = split_S;
+            d.split_H = split_H;
+            d.split_C = (g->max_deg + split_S - 1) / split_S;
+            L.any_split = true;
+        }
+        max_tasks = std::max(max_tasks, d.ntasks);
+        if (d.ne == 2) d.chunk = 32;  // one leaf over 32 root edges
+        else if (o.chunk) d.chunk = o.chunk;
+        else d.chunk = (uint32_t)std::max<unsigned long long>(1, std::min<unsigned long long>(8, d.ntasks / (warps * 64 + 1)));
+    }
+    L.heavy_cap = L.any_split ? (uint32_t)std::min<unsigned long long>(max_tasks, 1ull << 20) : 1u;
+    // buffer: plans | counts | per-plan queues | flags | stats | heavy counts | heavy lists
+    L.off_plans = 0;
+    L.off_counts = (sizeof(DevPlan) * nplans + 255) & ~(size_t)255;
+    L.off_queue = L.off_counts + ((8 * (size_t)nplans + 255) & ~(size_t)255);
+    L.off_flags = L.off_queue + ((8 * (size_t)nplans + 255) & ~(size_t)255);
+    L.off_stats = L.off_flags + 256;
+    L.off_hcnt = L.off_stats + 256;
+    L.off_hids = L.off_hcnt + ((4 * (size_t)nplans + 255) & ~(size_t)255);
+    L.bytes_zeroed = L.off_hids;
+    L.bytes = L.off_hids + (((size_t)L.heavy_cap * nplans * 4 + 255) & ~(size_t)255);
+    if (o.time_budget_s > 0) L.deadline = std::max<unsigned long long>(1, (unsigned long long)(o.time_budget_s * 1e9));
+    return SGE_OK;
+}
+
+// Stream-ordered: clear the counters, run phase 0 and (when roots may be
+// split) phase 1.  Capturable (no host synchronisation).
+sge_status enqueue_launch(sge_graph *g, const LaunchCfg &L, unsigned char *B, uint32_t *scratch, cudaStream_t s,
+                          uint32_t &launches) {
+    CUDA_TRY(cudaMemsetAsync(B + L.off_counts, 0, L.bytes_zeroed - L.off_counts, s));
+    DevGraph dg{g->d_off, g->d_adj, g->d_edges, g->n, g->m};
+    const DevPlan *dplans = reinterpret_cast<const DevPlan *>(B + L.off_plans);
+    unsigned long long *dcounts = reinterpret_cast<unsigned long long *>(B + L.off_counts);
+    unsigned long long *dqueue = reinterpret_cast<unsigned long long *>(B + L.off_queue);
+    uint32_t *dflags = reinterpret_cast<uint32_t *>(B + L.off_flags);
+    DevStats *dstats = reinterpret_cast<DevStats *>(B + L.off_stats);
+    uint32_t *dhcnt = reinterpret_cast<uint32_t *>(B + L.off_hcnt);
+    uint32_t *dhids = reinterpret_cast<uint32_t *>(B + L.off_hids);
+    launches = 0;
+    for (uint32_t phase = 0; phase < (L.any_split ? 2u : 1u); ++phase) {
+        if (phase == 1) CUDA_TRY(cudaMemsetAsync(dqueue, 0, 8 * (size_t)L.nplans, s));
+        if (L.want_stats)
+            count_kernel<true><<<(unsigned)L.blocks, L.threads, L.smem, s>>>(
+                dg, dplans, L.nplans, dqueue, dcounts, scratch, L.cap, L.nbufs, L.tw, L.tmode, L.deadline, dflags,
+                dstats, phase, dhcnt, dhids, L.heavy_cap);
+        else
+            count_kernel<false><<<(unsigned)L.blocks, L.threads, L.smem, s>>>(
+                dg, dplans, L.nplans, dqueue, dcounts, scratch, L.cap, L.nbufs, L.tw, L.tmode, L.deadline, dflags,
+                dstats, phase, dhcnt, dhids, L.heavy_cap);
+        CUDA_TRY(cudaGetLastError());
+        ++launches;
+    }
+    return SGE_OK;
+}
+
+sge_status finish_counts(const LaunchCfg &L, const unsigned long long *hc, uint32_t hflags, const DevStats &hs,
+                         float ms, uint32_t launches, std::chrono::steady_clock::time_point t_start,
+                         const sge_plan *const *plans, uint64_t *counts, uint64_t *instances, sge_stats *stats,
+                         const sge_count_opts &o) {
+    for (uint32_t i = 0; i < L.nplans; ++i) {
+        const uint64_t inst = hc[i];
+        counts[i] = inst * plans[i]->blob.count_multiplier;
+        if (instances) instances[i] = inst;
+    }
+    if (stats) {
+        stats->kernel_ms = ms;
+        stats->root_tasks = hs.roots;
+        stats->set_ops = hs.set_ops;
+        stats->alg_bytes = hs.alg_bytes;
+        stats->partial_matches = hs.partial;
+        stats->gpu_launches = launches;
+        stats->status_flags = hflags;
+        stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    }
+    if (hflags & FLAG_OVERFLOW) return fail(SGE_STACK_OVERFLOW, "a candidate list exceeded the per-level capacity %u", L.cap);
+    if (hflags & FLAG_TIMEOUT) return fail(SGE_TIMEOUT, "time budget of %.3f s exceeded; counts are partial", o.time_budget_s);
+    return SGE_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char *sge_version(void) { return "sge 0.1 (sm_103a, ABI 1)"; }
@@ -1306,143 +1454,115 @@ sge_status sge_count(sge_graph *g, const sge_plan *const *plans, uint32_t nplans
     sge_count_opts o{};
     if (opts) o = *opts;
     CUDA_TRY(cudaSetDevice(g->device));
-    std::vector<DevPlan> dps(nplans);
-    unsigned long long total = 0;
-    uint32_t nbufs = 1;
-    for (uint32_t i = 0; i < nplans; ++i) {
-        if (!plans[i]) return fail(SGE_BAD_INPUT, "plan %u is null", i);
-        dps[i] = plans[i]->dp;
-        dps[i].task_begin = total;
-        const unsigned long long all = (dps[i].root_kind == SGE_ROOT_ANY) ? 2ull * g->m : g->m;
-        const unsigned long long stride = o.root_stride > 1 ? o.root_stride : 1ull;
-        const unsigned long long offs = o.root_offset;
-        if (stride > 1 && offs >= stride) return fail(SGE_BAD_INPUT, "root_offset %llu >= root_stride %llu", offs, stride);
-        dps[i].root_stride = stride;
-        dps[i].root_offset = stride > 1 ? offs : 0;
-        dps[i].ntasks = all > dps[i].root_offset ? (all - dps[i].root_offset + stride - 1) / stride : 0;
-        total += dps[i].ntasks;
-        nbufs = std::max(nbufs, dps[i].nbufs);
-        if (dps[i].k > SGE_MAX_K) return fail(SGE_UNSUPPORTED, "plan %u has k=%u", i, dps[i].k);
-    }
-    const uint32_t wpb = o.warps_per_block ? std::min<uint32_t>(o.warps_per_block, 8) : 8;
-    const uint32_t threads = wpb * 32;
-    // pinned-list tables: a bitmap over all vertices when it fits in 4 KB, else a 512-slot hash
-    uint32_t tmode, tw;
-    if (g->n <= 32768u) { tmode = 1; tw = std::max<uint32_t>(32u, ((g->n + 31u) / 32u + 31u) & ~31u); }
-    else { tmode = 2; tw = 512; }
-    const size_t smem = warp_smem_bytes(tw) * wpb;
-    const bool want_stats = o.collect_counters != 0;
-    int bps = 0;
-    // static (plan copies) + dynamic shared memory exceed the 48 KB default: opt in
-    CUDA_TRY(cudaFuncSetAttribute(count_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CUDA_TRY(cudaFuncSetAttribute(count_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    if (want_stats) CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, count_kernel<true>, threads, smem));
-    else CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, count_kernel<false>, threads, smem));
-    if (o.blocks_per_sm) bps = std::min<int>(bps, (int)o.blocks_per_sm);
-    bps = std::max(bps, 1);
-    uint32_t cap = o.max_level_capacity ? o.max_level_capacity : std::max<uint32_t>(g->max_deg, 1);
-    cap = (cap + 31) & ~31u;
-    // fit the scratch into a quarter of free memory by trimming resident blocks
-    size_t free_b = 0, tot_b = 0;
-    CUDA_TRY(cudaMemGetInfo(&free_b, &tot_b));
-    size_t per_block = (size_t)wpb * nbufs * cap * sizeof(uint32_t);
-    size_t blocks = (size_t)g->num_sms * bps;
-    size_t budget = free_b / 4 + g->scratch_bytes;
-    while (blocks > (size_t)g->num_sms && blocks * per_block > budget) blocks -= g->num_sms;
-    if (blocks * per_block > budget) blocks = std::max<size_t>(1, budget / std::max<size_t>(per_block, 1));
-    sge_status st = ensure_scratch(g, blocks * per_block);
+    LaunchCfg L;
+    sge_status st = prepare_launch(g, plans, nplans, o, g->scratch_bytes, L);
     if (st != SGE_OK) return st;
-    // heavy-root splitting (plans with >= 3 enumerated levels): roots whose
-    // level-2 list may exceed 4·S candidates run as tasks of S candidates
-    const uint32_t split_S = 128, split_H = 4 * split_S;
-    bool any_split = false;
-    unsigned long long max_tasks = 1;
-    for (auto &d : dps) {
-        if (d.ne >= 3 && g->max_deg > split_H) {
-            d.split_S = split_S;
-            d.split_H = split_H;
-            d.split_C = (g->max_deg + split_S - 1) / split_S;
-            any_split = true;
-        }
-        max_tasks = std::max(max_tasks, d.ntasks);
-    }
-    const uint32_t heavy_cap = any_split ? (uint32_t)std::min<unsigned long long>(max_tasks, 1ull << 20) : 1u;
-    // batch buffer: plans | counts | per-plan queues | flags | stats | heavy counts | heavy lists
-    size_t off_plans = 0;
-    size_t off_counts = (sizeof(DevPlan) * nplans + 255) & ~(size_t)255;
-    size_t off_queue = off_counts + ((8 * (size_t)nplans + 255) & ~(size_t)255);
-    size_t off_flags = off_queue + ((8 * (size_t)nplans + 255) & ~(size_t)255);
-    size_t off_stats = off_flags + 256;
-    size_t off_hcnt = off_stats + 256;
-    size_t off_hids = off_hcnt + ((4 * (size_t)nplans + 255) & ~(size_t)255);
-    size_t bytes_zeroed = off_hids;
-    size_t bytes = off_hids + (((size_t)heavy_cap * nplans * 4 + 255) & ~(size_t)255);
-    st = ensure_batch(g, bytes);
-    if (st != SGE_OK) return st;
+    if ((st = ensure_scratch(g, L.scratch_bytes)) != SGE_OK) return st;
+    if ((st = ensure_batch(g, L.bytes)) != SGE_OK) return st;
     unsigned char *B = g->d_batch;
-    CUDA_TRY(cudaMemsetAsync(B + off_counts, 0, bytes_zeroed - off_counts, g->stream));
-    {
-        const unsigned long long warps = blocks * wpb;
-        for (auto &d : dps) {
-            if (d.ne == 2) d.chunk = 32;  // one leaf over 32 root edges
-            else if (o.chunk) d.chunk = o.chunk;
-            else d.chunk = (uint32_t)std::max<unsigned long long>(1, std::min<unsigned long long>(8, d.ntasks / (warps * 64 + 1)));
-        }
-    }
-    CUDA_TRY(cudaMemcpyAsync(B + off_plans, dps.data(), sizeof(DevPlan) * nplans, cudaMemcpyHostToDevice, g->stream));
-    unsigned long long deadline = 0;  // ns after each warp's start; 0 = none
-    DevGraph dg{g->d_off, g->d_adj, g->d_edges, g->n, g->m};
+    CUDA_TRY(cudaMemcpyAsync(B + L.off_plans, L.dps.data(), sizeof(DevPlan) * nplans, cudaMemcpyHostToDevice, g->stream));
     CUDA_TRY(cudaEventRecord(g->ev0, g->stream));
-    const DevPlan *dplans = reinterpret_cast<const DevPlan *>(B + off_plans);
-    unsigned long long *dcounts = reinterpret_cast<unsigned long long *>(B + off_counts);
-    unsigned long long *dqueue = reinterpret_cast<unsigned long long *>(B + off_queue);
-    uint32_t *dflags = reinterpret_cast<uint32_t *>(B + off_flags);
-    DevStats *dstats = reinterpret_cast<DevStats *>(B + off_stats);
-    uint32_t *dhcnt = reinterpret_cast<uint32_t *>(B + off_hcnt);
-    uint32_t *dhids = reinterpret_cast<uint32_t *>(B + off_hids);
-    if (o.time_budget_s > 0) deadline = std::max<unsigned long long>(1, (unsigned long long)(o.time_budget_s * 1e9));
     uint32_t launches = 0;
-    for (uint32_t phase = 0; phase < (any_split ? 2u : 1u); ++phase) {
-        if (phase == 1) CUDA_TRY(cudaMemsetAsync(dqueue, 0, 8 * (size_t)nplans, g->stream));
-        if (want_stats)
-            count_kernel<true><<<(unsigned)blocks, threads, smem, g->stream>>>(
-                dg, dplans, nplans, dqueue, dcounts, g->d_scratch, cap, nbufs, tw, tmode, deadline, dflags, dstats,
-                phase, dhcnt, dhids, heavy_cap);
-        else
-            count_kernel<false><<<(unsigned)blocks, threads, smem, g->stream>>>(
-                dg, dplans, nplans, dqueue, dcounts, g->d_scratch, cap, nbufs, tw, tmode, deadline, dflags, dstats,
-                phase, dhcnt, dhids, heavy_cap);
-        CUDA_TRY(cudaGetLastError());
-        ++launches;
-    }
+    if ((st = enqueue_launch(g, L, B, g->d_scratch, g->stream, launches)) != SGE_OK) return st;
     CUDA_TRY(cudaEventRecord(g->ev1, g->stream));
     std::vector<unsigned long long> hc(nplans);
     uint32_t hflags = 0;
     DevStats hs{};
-    CUDA_TRY(cudaMemcpyAsync(hc.data(), dcounts, 8 * nplans, cudaMemcpyDeviceToHost, g->stream));
-    CUDA_TRY(cudaMemcpyAsync(&hflags, dflags, 4, cudaMemcpyDeviceToHost, g->stream));
-    if (want_stats) CUDA_TRY(cudaMemcpyAsync(&hs, dstats, sizeof hs, cudaMemcpyDeviceToHost, g->stream));
+    CUDA_TRY(cudaMemcpyAsync(hc.data(), B + L.off_counts, 8 * nplans, cudaMemcpyDeviceToHost, g->stream));
+    CUDA_TRY(cudaMemcpyAsync(&hflags, B + L.off_flags, 4, cudaMemcpyDeviceToHost, g->stream));
+    if (L.want_stats) CUDA_TRY(cudaMemcpyAsync(&hs, B + L.off_stats, sizeof hs, cudaMemcpyDeviceToHost, g->stream));
     CUDA_TRY(cudaStreamSynchronize(g->stream));
     float ms = 0;
     cudaEventElapsedTime(&ms, g->ev0, g->ev1);
-    for (uint32_t i = 0; i < nplans; ++i) {
-        uint64_t inst = hc[i];
-        counts[i] = inst * plans[i]->blob.count_multiplier;
-        if (instances) instances[i] = inst;
-    }
-    if (stats) {
-        stats->kernel_ms = ms;
-        stats->root_tasks = hs.roots;
-        stats->set_ops = hs.set_ops;
-        stats->alg_bytes = hs.alg_bytes;
-        stats->partial_matches = hs.partial;
-        stats->gpu_launches = launches;
-        stats->status_flags = hflags;
-        stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
-    }
-    if (hflags & FLAG_OVERFLOW) return fail(SGE_STACK_OVERFLOW, "a candidate list exceeded the per-level capacity %u", cap);
-    if (hflags & FLAG_TIMEOUT) return fail(SGE_TIMEOUT, "time budget of %.3f s exceeded; counts are partial", o.time_budget_s);
+    return finish_counts(L, hc.data(), hflags, hs, ms, launches, t_start, plans, counts, instances, stats, o);
+}
+
+// ---- batches replayed from a captured CUDA graph ----
+struct sge_batch {
+    sge_graph *g = nullptr;
+    LaunchCfg L;
+    std::vector<const sge_plan *> plans;
+    sge_count_opts o{};
+    unsigned char *d_buf = nullptr;
+    uint32_t *d_scratch = nullptr;
+    unsigned char *h_res = nullptr;  // pinned: counts | flags | stats
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    uint32_t launches = 0;
+};
+
+sge_status sge_batch_destroy(sge_batch *b) {
+    if (!b) return SGE_OK;
+    cudaSetDevice(b->g->device);
+    cudaStreamSynchronize(b->g->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    cudaFree(b->d_buf);
+    cudaFree(b->d_scratch);
+    if (b->h_res) cudaFreeHost(b->h_res);
+    delete b;
     return SGE_OK;
+}
+
+sge_status sge_batch_create(sge_graph *g, const sge_plan *const *plans, uint32_t nplans, const sge_count_opts *opts,
+                            sge_batch **out) {
+    if (!g || !plans || nplans == 0 || !out) return fail(SGE_BAD_INPUT, "sge_batch_create: bad argument");
+    CUDA_TRY(cudaSetDevice(g->device));
+    sge_batch *b = new sge_batch();
+    b->g = g;
+    if (opts) b->o = *opts;
+    b->plans.assign(plans, plans + nplans);
+    auto bail = [&](sge_status st) { sge_batch_destroy(b); return st; };
+    sge_status st = prepare_launch(g, plans, nplans, b->o, 0, b->L);
+    if (st != SGE_OK) return bail(st);
+    cudaError_t e;
+    const size_t res_bytes = 8 * (size_t)nplans + 16 + sizeof(DevStats);
+    if ((e = cudaMalloc(&b->d_buf, b->L.bytes)) != cudaSuccess || (e = cudaMalloc(&b->d_scratch, std::max<size_t>(b->L.scratch_bytes, 4))) != cudaSuccess ||
+        (e = cudaMallocHost(&b->h_res, res_bytes)) != cudaSuccess || (e = cudaEventCreate(&b->ev0)) != cudaSuccess ||
+        (e = cudaEventCreate(&b->ev1)) != cudaSuccess)
+        return bail(fail(SGE_OOM, "sge_batch_create: %s", cudaGetErrorString(e)));
+    if ((e = cudaMemcpy(b->d_buf + b->L.off_plans, b->L.dps.data(), sizeof(DevPlan) * nplans, cudaMemcpyHostToDevice)) != cudaSuccess)
+        return bail(fail(SGE_CUDA_ERROR, "sge_batch_create: plan upload: %s", cudaGetErrorString(e)));
+    // capture: clear counters, both launch phases, read back counts/flags/stats
+    if ((e = cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+        return bail(fail(SGE_CUDA_ERROR, "stream capture: %s", cudaGetErrorString(e)));
+    st = enqueue_launch(g, b->L, b->d_buf, b->d_scratch, g->stream, b->launches);
+    if (st == SGE_OK) {
+        cudaMemcpyAsync(b->h_res, b->d_buf + b->L.off_counts, 8 * (size_t)nplans, cudaMemcpyDeviceToHost, g->stream);
+        cudaMemcpyAsync(b->h_res + 8 * (size_t)nplans, b->d_buf + b->L.off_flags, 4, cudaMemcpyDeviceToHost, g->stream);
+        cudaMemcpyAsync(b->h_res + 8 * (size_t)nplans + 16, b->d_buf + b->L.off_stats, sizeof(DevStats),
+                        cudaMemcpyDeviceToHost, g->stream);
+    }
+    e = cudaStreamEndCapture(g->stream, &b->graph);
+    if (st != SGE_OK) return bail(st);
+    if (e != cudaSuccess) return bail(fail(SGE_CUDA_ERROR, "stream capture: %s", cudaGetErrorString(e)));
+    if ((e = cudaGraphInstantiate(&b->exec, b->graph, 0)) != cudaSuccess)
+        return bail(fail(SGE_CUDA_ERROR, "graph instantiate: %s", cudaGetErrorString(e)));
+    *out = b;
+    return SGE_OK;
+}
+
+sge_status sge_batch_run(sge_batch *b, uint64_t *counts, uint64_t *instances, sge_stats *stats) {
+    auto t_start = std::chrono::steady_clock::now();
+    if (!b || !counts) return fail(SGE_BAD_INPUT, "sge_batch_run: null argument");
+    sge_graph *g = b->g;
+    CUDA_TRY(cudaSetDevice(g->device));
+    CUDA_TRY(cudaEventRecord(b->ev0, g->stream));
+    CUDA_TRY(cudaGraphLaunch(b->exec, g->stream));
+    CUDA_TRY(cudaEventRecord(b->ev1, g->stream));
+    CUDA_TRY(cudaStreamSynchronize(g->stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+    const uint32_t n = b->L.nplans;
+    uint32_t hflags = 0;
+    DevStats hs{};
+    memcpy(&hflags, b->h_res + 8 * (size_t)n, 4);
+    memcpy(&hs, b->h_res + 8 * (size_t)n + 16, sizeof hs);
+    return finish_counts(b->L, reinterpret_cast<const unsigned long long *>(b->h_res), hflags, hs, ms, b->launches,
+                         t_start, b->plans.data(), counts, instances, stats, b->o);
 }
 
 sge_status sge_count_host(const uint32_t *offsets, const uint32_t *nbrs, uint32_t n, uint64_t nnz,

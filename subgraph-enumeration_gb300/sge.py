@@ -142,6 +142,9 @@ SIGNATURES = {
                                 _P(C.c_float)]),
     "sge_plan_pattern_learned": (C.c_int, [u32, u32, _P(u32), _P(GraphStats), _P(PlanOpts), C.c_void_p, u32,
                                            _P(PlanBlob)]),
+    "sge_batch_create": (C.c_int, [C.c_void_p, _P(C.c_void_p), u32, _P(CountOpts), _P(C.c_void_p)]),
+    "sge_batch_run": (C.c_int, [C.c_void_p, _P(u64), _P(u64), _P(Stats)]),
+    "sge_batch_destroy": (C.c_int, [C.c_void_p]),
     "sge_count_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, u32, u64, u32, _P(PlanBlob), u32, C.c_void_p,
                                     C.c_void_p]),
 }
@@ -474,10 +477,68 @@ class Engine:
             for h in handles:
                 lib().sge_plan_destroy(h)
 
+    def batch(self, plans: list[PlanBlob], stats: bool = False, **opts) -> "Batch":
+        """A batch captured into a CUDA graph (replay with Batch.run)."""
+        return Batch(self, plans, stats, **opts)
+
     def close(self) -> None:
         if getattr(self, "_h", None):
             lib().sge_graph_destroy(self._h)
             self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """sge_batch: plans uploaded once, launch sequence captured into a CUDA graph."""
+
+    def __init__(self, engine: Engine, plans: list[PlanBlob], stats: bool = False, time_budget_s: float = 0.0,
+                 blocks_per_sm: int = 0, warps_per_block: int = 0, chunk: int = 0, root_stride: int = 1,
+                 root_offset: int = 0):
+        self.engine = engine
+        self.n = len(plans)
+        self._ph = []
+        for b in plans:
+            ph = C.c_void_p()
+            _check(lib().sge_plan_create(C.byref(b), C.byref(ph)))
+            self._ph.append(ph)
+        arr = (C.c_void_p * self.n)(*[h.value for h in self._ph])
+        o = CountOpts(blocks_per_sm, warps_per_block, chunk, time_budget_s, 0, root_stride, root_offset, int(stats))
+        h = C.c_void_p()
+        try:
+            _check(lib().sge_batch_create(engine._h, arr, self.n, C.byref(o), C.byref(h)))
+        except SgeError:
+            self._free_plans()
+            raise
+        self._h = h
+
+    def run(self):
+        counts = (u64 * self.n)()
+        inst = (u64 * self.n)()
+        st = Stats()
+        _check(lib().sge_batch_run(self._h, counts, inst, C.byref(st)))
+        return list(counts), list(inst), st.as_dict()
+
+    def _free_plans(self):
+        for h in self._ph:
+            lib().sge_plan_destroy(h)
+        self._ph = []
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sge_batch_destroy(self._h)
+            self._h = None
+        self._free_plans()
 
     def __enter__(self):
         return self
