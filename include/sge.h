@@ -178,7 +178,7 @@ typedef struct sge_plan sge_plan;
 /* ---- diagnostics ---- */
 /* sizeof of the ABI structs, for binding checks: 0 sge_plan_blob,
  * 1 sge_plan_opts, 2 sge_count_opts, 3 sge_stats, 4 sge_graph_info,
- * 5 sge_graph_stats. */
+ * 5 sge_graph_stats, 6 sge_trie. */
 size_t sge_struct_size(int which);
 const char *sge_last_error(void);
 const char *sge_version(void);
@@ -293,6 +293,44 @@ sge_status sge_batch_create(sge_graph *g, const sge_plan *const *plans, uint32_t
                             sge_batch **out);
 sge_status sge_batch_run(sge_batch *b, uint64_t *counts, uint64_t *instances, sge_stats *stats);
 sge_status sge_batch_destroy(sge_batch *b);
+/* ---- enumeration and bag relations (nodeJoin + buildTrie, matching/join.cpp:309-421,1713-1717;
+ *      TrieLevel::buildTrieFromSortedMatchesBatch, relation/relation.cpp:340-379) ---- */
+/* Writes every match of p (one per automorphism class: the representative
+ * the plan's restrictions keep) as k uint32 vertex ids in pattern-vertex
+ * order into the device buffer d_out (capacity rows).  *n_matches receives
+ * the number of matches; more than capacity returns SGE_OOM (rows past
+ * capacity are dropped).  The plan must have a one-level tail (no IEP). */
+sge_status sge_enumerate(sge_graph *g, const sge_plan *p, uint32_t *d_out, uint64_t capacity, uint64_t *n_matches);
+/* Automorphisms of a pattern: naut rows of k vertex images (cap rows max). */
+sge_status sge_pattern_automorphisms(uint32_t k, uint32_t m, const uint32_t *edges, uint8_t *out, uint32_t cap,
+                                     uint32_t *naut);
+/* Replaces each device row (k ids, pattern-vertex order) by the
+ * lexicographically smallest of its images under the automorphisms (perms:
+ * host array naut×k), i.e. a plan-independent form of each instance. */
+sge_status sge_canonicalize(uint32_t *d_tuples, uint64_t n, uint32_t k, const uint8_t *perms, uint32_t naut);
+/* Lexicographic sort of n device rows of `arity` uint32 (LSD radix sort). */
+sge_status sge_sort_tuples(uint32_t *d_tuples, uint64_t n, uint32_t arity);
+/* Trie of sorted rows: level l holds level_len[l] values (device);
+ * node p of level l < arity-1 owns children [child[l][p], child[l][p+1]). */
+#define SGE_TRIE_MAX_LEVELS 16u
+typedef struct sge_trie {
+    uint32_t arity;
+    uint64_t level_len[SGE_TRIE_MAX_LEVELS];
+    uint32_t *values[SGE_TRIE_MAX_LEVELS];
+    unsigned long long *child[SGE_TRIE_MAX_LEVELS];
+} sge_trie;
+sge_status sge_trie_build(const uint32_t *d_sorted, uint64_t n, uint32_t arity, sge_trie *out);
+sge_status sge_trie_free(sge_trie *t);
+/* Copies level `level` of a trie to host: level_len[level] values and, below
+ * the last level, level_len[level]+1 child offsets (child may be NULL). */
+sge_status sge_trie_copy_level(const sge_trie *t, uint32_t level, uint32_t *values, unsigned long long *child);
+/* The sorted instance set (what -r writes; the reference never writes one):
+ * one row per instance, each row the lexicographically smallest image of an
+ * embedding under the automorphisms, rows sorted.  p must have a one-level
+ * tail.  *n_rows receives the instance count; SGE_OOM when above cap_rows. */
+sge_status sge_match_set(sge_graph *g, const sge_plan *p, uint32_t k, uint32_t m, const uint32_t *edges,
+                         uint32_t *host_out, uint64_t cap_rows, uint64_t *n_rows);
+
 /* End-to-end convenience: host CSR in, counts out (H2D copy, count, D2H read
  * and release all inside the call). */
 sge_status sge_count_host(const uint32_t *offsets, const uint32_t *nbrs, uint32_t num_vertices,

@@ -45,6 +45,8 @@ def lib() -> C.CDLL:
         L.oracle_count_plan.restype = u64
         L.oracle_count_plan.argtypes = [_P(u32), _P(u32), u32, C.c_void_p, C.c_int, u64, u64, _P(u64)]
         L.oracle_max_threads.restype = C.c_int
+        L.oracle_list_embeddings.restype = u64
+        L.oracle_list_embeddings.argtypes = [_P(u32), _P(u32), u32, u32, u32, _P(u32), _P(u32), u64]
         _lib = L
     return _lib
 
@@ -120,3 +122,32 @@ def count_plan(offsets, nbrs, blob, threads: int = 0, stride: int = 1, offset: i
 
 def max_threads() -> int:
     return int(lib().oracle_max_threads())
+
+
+def list_embeddings(offsets, nbrs, k: int, edges, cap: int = 1 << 22) -> np.ndarray:
+    """Every embedding as k ids in pattern-vertex order (brute force)."""
+    off, nb, e = _arr(offsets), _arr(nbrs), _arr(edges).reshape(-1)
+    out = np.zeros(cap * k, np.uint32)
+    n = int(lib().oracle_list_embeddings(_p(off), _p(nb), off.size - 1, k, e.size // 2, _p(e), _p(out), cap))
+    if n > cap:
+        raise ValueError(f"{n} embeddings exceed cap {cap}")
+    return out[: n * k].reshape(n, k)
+
+
+def canonical_instances(emb: np.ndarray, perms: np.ndarray) -> np.ndarray:
+    """One row per instance: the lexicographically smallest image of an
+    embedding under the automorphisms, unique, sorted."""
+    imgs = np.stack([emb[:, p] for p in perms])           # naut × n × k
+    # lexicographic minimum over automorphisms, row by row
+    best = imgs[0].copy()
+    for a in range(1, imgs.shape[0]):
+        cand = imgs[a]
+        less = np.zeros(len(best), bool)
+        decided = np.zeros(len(best), bool)
+        for j in range(best.shape[1]):
+            lt = (cand[:, j] < best[:, j]) & ~decided
+            gt = (cand[:, j] > best[:, j]) & ~decided
+            less |= lt
+            decided |= lt | gt
+        best[less] = cand[less]
+    return np.unique(best, axis=0)

@@ -455,3 +455,58 @@ int oracle_max_threads(void) {
     return 1;
 #endif
 }
+
+/* Lists every embedding (injective homomorphism) as k ids in pattern-vertex
+ * order, by the same DFS as oracle_bruteforce_embeddings (single thread).
+ * Returns the number of embeddings; rows past cap are not written. */
+uint64_t oracle_list_embeddings(const uint32_t *off, const uint32_t *nb, uint32_t n, uint32_t k, uint32_t m,
+                                const uint32_t *edges, uint32_t *out, uint64_t cap) {
+    uint32_t adj[32] = {0};
+    for (uint32_t i = 0; i < m; ++i) { adj[edges[2 * i]] |= 1u << edges[2 * i + 1]; adj[edges[2 * i + 1]] |= 1u << edges[2 * i]; }
+    uint32_t order[32], seen = 0, best = 0;
+    for (uint32_t u = 1; u < k; ++u) if (__builtin_popcount(adj[u]) > __builtin_popcount(adj[best])) best = u;
+    order[0] = best; seen = 1u << best;
+    for (uint32_t i = 1; i < k; ++i) {
+        int bv = -1, bs = -1;
+        for (uint32_t u = 0; u < k; ++u) {
+            if ((seen >> u) & 1u) continue;
+            int s = __builtin_popcount(adj[u] & seen);
+            if (s > 0 && s > bs) { bs = s; bv = (int)u; }
+        }
+        if (bv < 0) return 0;
+        order[i] = (uint32_t)bv; seen |= 1u << bv;
+    }
+    uint32_t back[32], first[32];
+    for (uint32_t i = 0; i < k; ++i) {
+        back[i] = 0;
+        for (uint32_t j = 0; j < i; ++j) if (pat_edge(adj, order[i], order[j])) back[i] |= 1u << j;
+        first[i] = back[i] ? (uint32_t)__builtin_ctz(back[i]) : 0;
+    }
+    uint64_t total = 0;
+    for (uint32_t r = 0; r < n; ++r) {
+        uint32_t mm[32], it[32];
+        int lv = 1;
+        mm[0] = r;
+        it[1] = off[mm[first[1]]];
+        while (lv >= 1) {
+            uint32_t p = mm[first[lv]];
+            if (it[lv] >= off[p + 1]) { --lv; continue; }
+            uint32_t x = nb[it[lv]++];
+            int ok = 1;
+            for (int j = 0; j < lv && ok; ++j) if (mm[j] == x) ok = 0;
+            for (uint32_t msk = back[lv] & ~(1u << first[lv]); msk && ok; msk &= msk - 1)
+                if (!has_edge(off, nb, mm[__builtin_ctz(msk)], x)) ok = 0;
+            if (!ok) continue;
+            mm[lv] = x;
+            if (lv + 1 == (int)k) {
+                if (total < cap)
+                    for (uint32_t i = 0; i < k; ++i) out[total * k + order[i]] = mm[i];
+                ++total;
+                continue;
+            }
+            ++lv;
+            it[lv] = off[mm[first[lv]]];
+        }
+    }
+    return total;
+}

@@ -4,8 +4,12 @@
 //   [-t threads]  [--help|-h]
 // plus additive flags: --device N, --batch LIST (one pattern path per line,
 // counted in one persistent launch), --seed S.
-// Like the reference, -r redirects the text log to a file.  Planning runs on
-// the host; the join runs on the GPU through libsge.
+// Like the reference, -r redirects the text log to a file; it also writes the
+// sorted instance set to <file>.matches (<file>.<i>.matches for --batch), one
+// row per instance in the row format of the reference's storeMatches
+// (matching/join.cpp:1703-1711: the row count, then the ids of each row
+// followed by a space).  The reference itself never writes this set.
+// Planning runs on the host; the join runs on the GPU through libsge.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -92,6 +96,8 @@ int main(int argc, char **argv) {
     auto t0 = std::chrono::steady_clock::now();
     std::vector<sge_plan *> plans;
     std::vector<sge_plan_blob> blobs;
+    std::vector<std::vector<uint32_t>> pedges;
+    std::vector<uint32_t> pk;
     for (auto &qp : queries) {
         uint32_t k, m, edges[2 * SGE_MAX_K * SGE_MAX_K];
         if (sge_load_pattern_file(qp.c_str(), &k, &m, edges) != SGE_OK) {
@@ -115,6 +121,8 @@ int main(int argc, char **argv) {
         }
         blobs.push_back(b);
         plans.push_back(p);
+        pedges.emplace_back(edges, edges + 2 * m);
+        pk.push_back(k);
     }
     double plan_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     for (size_t i = 0; i < blobs.size(); ++i) {
@@ -148,6 +156,37 @@ int main(int argc, char **argv) {
     out << "Number of intersections: " << st.set_ops << std::endl;
     out << "Execution Time: " << exec_s << std::endl;
     out << "GPU time (ms): " << st.kernel_ms << std::endl;
+    if (!a.r.empty()) {
+        for (size_t i = 0; i < plans.size(); ++i) {
+            const uint32_t k = pk[i], m = (uint32_t)(pedges[i].size() / 2);
+            sge_plan_opts po{};
+            po.use_iep = 0;
+            po.max_tail = 1;
+            sge_plan_blob eb;
+            sge_plan *ep = nullptr;
+            if (sge_plan_pattern(k, m, pedges[i].data(), g, &po, &eb) != SGE_OK || sge_plan_create(&eb, &ep) != SGE_OK) {
+                std::cout << "error: " << sge_last_error() << std::endl;
+                return 1;
+            }
+            std::vector<uint32_t> rows((size_t)std::max<uint64_t>(inst[i], 1) * k);
+            uint64_t n = 0;
+            if (sge_match_set(g, ep, k, m, pedges[i].data(), rows.data(), inst[i], &n) != SGE_OK) {
+                std::cout << "error: " << sge_last_error() << std::endl;
+                return 1;
+            }
+            sge_plan_destroy(ep);
+            const std::string path = a.r + (plans.size() > 1 ? "." + std::to_string(i) : std::string()) + ".matches";
+            FILE *f = fopen(path.c_str(), "w");
+            if (!f) { std::cout << "Can not create file " << path << "!" << std::endl; return 1; }
+            fprintf(f, "%llu\n", (unsigned long long)n);
+            for (uint64_t r = 0; r < n; ++r) {
+                for (uint32_t j = 0; j < k; ++j) fprintf(f, "%u ", rows[r * k + j]);
+                fputc('\n', f);
+            }
+            fclose(f);
+            out << "Matches written: " << path << std::endl;
+        }
+    }
     for (auto *p : plans) sge_plan_destroy(p);
     sge_graph_destroy(g);
     sge_free_host(off);

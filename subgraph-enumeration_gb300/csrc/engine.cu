@@ -68,6 +68,7 @@ struct DevPlan {
     uint32_t split_H;                             // roots whose level-2 bound exceeds this are deferred
     uint32_t split_S;                             // level-2 candidates per deferred task (0 = never defer)
     uint32_t split_C;                             // deferred tasks per heavy root (max degree / S, rounded up)
+    uint32_t order_[SGE_MAX_K];                   // pattern vertex of each level (enumeration output order)
     uint32_t hoist_at[SGE_MAX_K];                 // level after whose match a hoisted list is computed
 };
 
@@ -1011,6 +1012,99 @@ __global__ void __launch_bounds__(256, 3) count_kernel(DevGraph g, const DevPlan
     }
 }
 
+
+// ------------------------------------------------------------ enumeration --
+// Writes every match of a plan (all k levels enumerated, no counting tail)
+// as k vertex ids in pattern-vertex order: the tuples of nodeJoin /
+// globalJoin before buildTrie (matching/join.cpp:309-421,1202-1420) and, for
+// the whole pattern, the embedding set -r writes.  A warp owns one root edge;
+// the last level's candidates are emitted 32 at a time with one atomicAdd of
+// the output cursor per chunk.
+__global__ void __launch_bounds__(256) enum_kernel(DevGraph g, const DevPlan *__restrict__ plan,
+                                                   unsigned long long *queue, uint32_t *scratch, uint32_t cap,
+                                                   uint32_t bufs_per_warp, uint32_t *flags, uint32_t *out,
+                                                   unsigned long long out_cap, unsigned long long *out_n) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const uint32_t lane = lane_id();
+    const uint32_t wib = threadIdx.x >> 5;
+    __shared__ DevPlan Psh[8];
+    DevPlan &P = Psh[wib];
+    const size_t gwarp = (size_t)blockIdx.x * (blockDim.x >> 5) + wib;
+    Ctx<false> c;
+    c.g = g;
+    c.buf = scratch + gwarp * (size_t)bufs_per_warp * cap;
+    c.cap = cap;
+    c.flags = flags;
+    c.set_ops = c.alg_bytes = c.partial = 0;
+    c.tstart = 0;
+    c.deadline = 0;
+    WarpState &W = setup_warp(smem_raw, wib, 0u, 0u, c);
+    {
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(plan);
+        uint32_t *dst = reinterpret_cast<uint32_t *>(&P);
+        for (uint32_t w = lane; w < sizeof(DevPlan) / 4; w += 32) dst[w] = src[w];
+        __syncwarp();
+    }
+    const uint32_t k = P.k, last = k - 1;
+    while (true) {
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(queue, 1ull);
+        t = __shfl_sync(FULL_MASK, t, 0);
+        if (t >= P.ntasks) break;
+        if (*(volatile uint32_t *)flags & FLAG_OVERFLOW) break;
+        const uint2 e = root_edge(g, P, t);
+        set_match(g, W, 0, e.x);
+        set_match(g, W, 1, e.y);
+        uint32_t lv = 2;
+        bool ok = build_level_wcoj(P, W, c, lv);
+        if (ok) { __syncwarp(); if (lane == 0) W.pos[lv] = 0; __syncwarp(); }
+        while (ok) {
+            if (lv == last) {
+                const uint32_t n = W.cnt[lv];
+                const uint32_t *lst = W.list[lv];
+                for (uint32_t b0 = 0; b0 < n; b0 += 32) {
+                    const uint32_t idx = b0 + lane;
+                    bool valid = idx < n;
+                    const uint32_t x = valid ? lst[idx] : 0u;
+                    if (valid) valid = !excluded(P, W, lv, x);
+                    const uint32_t bal = __ballot_sync(FULL_MASK, valid);
+                    unsigned long long base = 0;
+                    if (lane == 0 && bal) base = atomicAdd(out_n, (unsigned long long)__popc(bal));
+                    base = __shfl_sync(FULL_MASK, base, 0);
+                    if (valid) {
+                        const unsigned long long row = base + __popc(bal & ((1u << lane) - 1u));
+                        if (row < out_cap) {
+                            uint32_t *o = out + row * k;
+                            for (uint32_t l = 0; l < last; ++l) o[P.order_[l]] = W.m[l];
+                            o[P.order_[last]] = x;
+                        }
+                    }
+                }
+                if (lv == 2) break;
+                --lv;
+                continue;
+            }
+            const uint32_t pos = W.pos[lv];
+            if (pos >= W.cnt[lv]) {
+                if (lv == 2) break;
+                --lv;
+                continue;
+            }
+            const uint32_t x = W.list[lv][pos];
+            __syncwarp();
+            if (lane == 0) W.pos[lv] = pos + 1;
+            __syncwarp();
+            if (excluded(P, W, lv, x)) continue;
+            set_match(g, W, lv, x);
+            ++lv;
+            if (!build_level_wcoj(P, W, c, lv)) { ok = false; break; }
+            __syncwarp();
+            if (lane == 0) W.pos[lv] = 0;
+            __syncwarp();
+        }
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -1122,6 +1216,7 @@ void to_devplan(const sge_plan_blob &b, DevPlan &d) {
     d.mult = b.count_multiplier;
     d.chunk = 1;
     d.split_par = b.num_enum >= 3 ? (b.parents[2] & 3u) : 0u;
+    for (uint32_t i = 0; i < SGE_MAX_K; ++i) d.order_[i] = b.order[i];
     d.split_S = 0;  // set per graph in sge_count
 }
 
@@ -1563,6 +1658,56 @@ sge_status sge_batch_run(sge_batch *b, uint64_t *counts, uint64_t *instances, sg
     memcpy(&hs, b->h_res + 8 * (size_t)n + 16, sizeof hs);
     return finish_counts(b->L, reinterpret_cast<const unsigned long long *>(b->h_res), hflags, hs, ms, b->launches,
                          t_start, b->plans.data(), counts, instances, stats, b->o);
+}
+
+sge_status sge_enumerate(sge_graph *g, const sge_plan *p, uint32_t *d_out, uint64_t capacity, uint64_t *n_matches) {
+    if (!g || !p || !n_matches || (!d_out && capacity)) return fail(SGE_BAD_INPUT, "sge_enumerate: null argument");
+    if (p->blob.tail_len != 1)
+        return fail(SGE_BAD_INPUT, "sge_enumerate needs a plan with a one-level tail (plan it without IEP)");
+    CUDA_TRY(cudaSetDevice(g->device));
+    DevPlan d = p->dp;
+    d.ne = d.k;  // every level is enumerated
+    d.hoist_mask = 0;
+    d.root_stride = 1;
+    d.root_offset = 0;
+    d.ntasks = (d.root_kind == SGE_ROOT_ANY) ? 2ull * g->m : g->m;
+    d.nbufs = d.k;
+    const uint32_t wpb = 8, threads = 256;
+    const size_t smem = warp_smem_bytes(0) * wpb;
+    CUDA_TRY(cudaFuncSetAttribute(enum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int bps = 0;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, enum_kernel, threads, smem));
+    bps = std::max(bps, 1);
+    const uint32_t cap = (std::max<uint32_t>(g->max_deg, 1) + 31) & ~31u;
+    size_t free_b = 0, tot_b = 0;
+    CUDA_TRY(cudaMemGetInfo(&free_b, &tot_b));
+    const size_t per_block = (size_t)wpb * d.nbufs * cap * sizeof(uint32_t);
+    size_t blocks = (size_t)g->num_sms * bps;
+    const size_t budget = free_b / 4 + g->scratch_bytes;
+    while (blocks > 1 && blocks * per_block > budget) --blocks;
+    sge_status st = ensure_scratch(g, blocks * per_block);
+    if (st != SGE_OK) return st;
+    st = ensure_batch(g, sizeof(DevPlan) + 256);
+    if (st != SGE_OK) return st;
+    unsigned char *B = g->d_batch;
+    unsigned long long *dq = reinterpret_cast<unsigned long long *>(B + sizeof(DevPlan));
+    unsigned long long *dn = dq + 1;
+    uint32_t *dflags = reinterpret_cast<uint32_t *>(dq + 2);
+    CUDA_TRY(cudaMemsetAsync(dq, 0, 24, g->stream));
+    CUDA_TRY(cudaMemcpyAsync(B, &d, sizeof(DevPlan), cudaMemcpyHostToDevice, g->stream));
+    DevGraph dg{g->d_off, g->d_adj, g->d_edges, g->n, g->m};
+    enum_kernel<<<(unsigned)blocks, threads, smem, g->stream>>>(dg, reinterpret_cast<const DevPlan *>(B), dq,
+                                                                g->d_scratch, cap, d.nbufs, dflags, d_out, capacity, dn);
+    CUDA_TRY(cudaGetLastError());
+    unsigned long long n = 0;
+    uint32_t flags = 0;
+    CUDA_TRY(cudaMemcpyAsync(&n, dn, 8, cudaMemcpyDeviceToHost, g->stream));
+    CUDA_TRY(cudaMemcpyAsync(&flags, dflags, 4, cudaMemcpyDeviceToHost, g->stream));
+    CUDA_TRY(cudaStreamSynchronize(g->stream));
+    *n_matches = n;
+    if (flags & FLAG_OVERFLOW) return fail(SGE_STACK_OVERFLOW, "a candidate list exceeded the per-level capacity");
+    if (n > capacity) return fail(SGE_OOM, "%llu matches exceed the output capacity %llu", n, (unsigned long long)capacity);
+    return SGE_OK;
 }
 
 sge_status sge_count_host(const uint32_t *offsets, const uint32_t *nbrs, uint32_t n, uint64_t nnz,

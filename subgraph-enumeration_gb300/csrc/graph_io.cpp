@@ -146,6 +146,7 @@ size_t sge_struct_size(int which) {
         case 3: return sizeof(sge_stats);
         case 4: return sizeof(sge_graph_info);
         case 5: return sizeof(sge_graph_stats);
+        case 6: return sizeof(sge_trie);
         default: return 0;
     }
 }

@@ -687,3 +687,17 @@ extern "C" sge_status sge_plan_pattern_learned(uint32_t k, uint32_t m, const uin
     *out = cands[best].blob;
     return SGE_OK;
 }
+
+extern "C" sge_status sge_pattern_automorphisms(uint32_t k, uint32_t m, const uint32_t *edges, uint8_t *out,
+                                                uint32_t cap, uint32_t *naut) {
+    if (!out || !naut) return fail(SGE_BAD_INPUT, "sge_pattern_automorphisms: null argument");
+    Pattern p;
+    sge_status st = make_pattern(k, m, edges, p);
+    if (st != SGE_OK) return st;
+    std::vector<Perm> aut;
+    if (!automorphisms(p, aut, cap)) return fail(SGE_UNSUPPORTED, "more than %u automorphisms", cap);
+    for (size_t a = 0; a < aut.size(); ++a)
+        for (uint32_t j = 0; j < k; ++j) out[a * k + j] = aut[a][j];
+    *naut = (uint32_t)aut.size();
+    return SGE_OK;
+}

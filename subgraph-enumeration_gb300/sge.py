@@ -95,6 +95,10 @@ class GraphStats(C.Structure):
                 ("moments", C.c_double * (SGE_MAX_K + 2)), ("clustering", C.c_double), ("max_degree", C.c_double)]
 
 
+class Trie(C.Structure):
+    _fields_ = [("arity", u32), ("level_len", u64 * 16), ("values", C.c_void_p * 16), ("child", C.c_void_p * 16)]
+
+
 class GraphInfo(C.Structure):
     _fields_ = [("num_vertices", u32), ("num_directed_edges", u64), ("max_degree", u32), ("device_bytes", u64)]
 
@@ -145,6 +149,14 @@ SIGNATURES = {
     "sge_batch_create": (C.c_int, [C.c_void_p, _P(C.c_void_p), u32, _P(CountOpts), _P(C.c_void_p)]),
     "sge_batch_run": (C.c_int, [C.c_void_p, _P(u64), _P(u64), _P(Stats)]),
     "sge_batch_destroy": (C.c_int, [C.c_void_p]),
+    "sge_enumerate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, u64, _P(u64)]),
+    "sge_pattern_automorphisms": (C.c_int, [u32, u32, _P(u32), _P(C.c_uint8), u32, _P(u32)]),
+    "sge_canonicalize": (C.c_int, [C.c_void_p, u64, u32, _P(C.c_uint8), u32]),
+    "sge_sort_tuples": (C.c_int, [C.c_void_p, u64, u32]),
+    "sge_trie_build": (C.c_int, [C.c_void_p, u64, u32, _P(Trie)]),
+    "sge_trie_free": (C.c_int, [_P(Trie)]),
+    "sge_trie_copy_level": (C.c_int, [_P(Trie), u32, _P(u32), _P(u64)]),
+    "sge_match_set": (C.c_int, [C.c_void_p, C.c_void_p, u32, u32, _P(u32), _P(u32), u64, _P(u64)]),
     "sge_count_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, u32, u64, u32, _P(PlanBlob), u32, C.c_void_p,
                                     C.c_void_p]),
 }
@@ -477,6 +489,26 @@ class Engine:
             for h in handles:
                 lib().sge_plan_destroy(h)
 
+    def match_set(self, pattern: PatternGraph, exploration: bool = False, max_rows: int = 1 << 26) -> np.ndarray:
+        """Sorted instance set: one row per instance (canonical image under the
+        automorphisms), pattern-vertex order."""
+        b = plan(pattern, self, iep=False, exploration=exploration)
+        ph = C.c_void_p()
+        _check(lib().sge_plan_create(C.byref(b), C.byref(ph)))
+        try:
+            n = u64()
+            e = pattern.flat()
+            # size from the count first
+            _, inst, _ = self.count([b])
+            rows = int(inst[0])
+            if rows > max_rows:
+                raise SgeError(2, f"{rows} instances exceed max_rows={max_rows}")
+            out = np.zeros(max(rows, 1) * pattern.k, np.uint32)
+            _check(lib().sge_match_set(self._h, ph, pattern.k, pattern.m, _u32p(e), _u32p(out), rows, C.byref(n)))
+            return out[: n.value * pattern.k].reshape(n.value, pattern.k)
+        finally:
+            lib().sge_plan_destroy(ph)
+
     def batch(self, plans: list[PlanBlob], stats: bool = False, **opts) -> "Batch":
         """A batch captured into a CUDA graph (replay with Batch.run)."""
         return Batch(self, plans, stats, **opts)
@@ -551,6 +583,30 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def sort_tuples_device(ptr: int, n: int, arity: int) -> None:
+    """Lexicographic LSD radix sort of n device rows (uint32 × arity) in place."""
+    _check(lib().sge_sort_tuples(C.c_void_p(ptr), n, arity))
+
+
+def trie_build_device(ptr: int, n: int, arity: int) -> Trie:
+    t = Trie()
+    _check(lib().sge_trie_build(C.c_void_p(ptr), n, arity, C.byref(t)))
+    return t
+
+
+def trie_level(t: Trie, level: int) -> tuple[np.ndarray, np.ndarray | None]:
+    n = int(t.level_len[level])
+    vals = np.zeros(max(n, 1), np.uint32)
+    child = np.zeros(n + 1, np.uint64) if level + 1 < t.arity else None
+    _check(lib().sge_trie_copy_level(C.byref(t), level, _u32p(vals),
+                                     child.ctypes.data_as(C.POINTER(u64)) if child is not None else None))
+    return vals[:n], child
+
+
+def trie_free(t: Trie) -> None:
+    lib().sge_trie_free(C.byref(t))
 
 
 def count_host(graph: DataGraph, plans: list[PlanBlob], stats: bool = False):

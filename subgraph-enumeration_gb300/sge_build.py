@@ -25,7 +25,7 @@ ORACLE_OUT = ORACLE / "_build"
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_SRCS = ["planner.cpp", "graph_io.cpp", "generators.cpp"]
-CU_SRCS = ["engine.cu", "mlp.cu"]
+CU_SRCS = ["engine.cu", "mlp.cu", "relation.cu"]
 
 
 def _run(cmd: list[str], cwd: Path | None = None) -> None:

@@ -43,3 +43,24 @@ def test_cli_missing_file_exits_1(tmp_path):
     out = subprocess.run([str(PKG / "_build" / "graph_mining_system"), "-q", str(tmp_path / "nope"), "-d",
                           str(GOLDEN / "ca_netscience.el")], capture_output=True, text=True, timeout=60)
     assert out.returncode == 1 and "Can not open file" in out.stdout
+
+
+def test_cli_result_file_holds_sorted_instance_set(sge, oracle, patterns, graphs, tmp_path):
+    import numpy as np
+    from test_gpu_relations import sge_perms
+    q = tmp_path / "q.txt"
+    p = pattern_of(sge, patterns, "light_query/p4")
+    q.write_text(p.text())
+    res = tmp_path / "run.log"
+    out = subprocess.run([str(PKG / "_build" / "graph_mining_system"), "-q", str(q), "-d",
+                          str(GOLDEN / "ca_netscience.el"), "-u", "-r", str(res)], capture_output=True, text=True,
+                         timeout=300)
+    assert out.returncode == 0, out.stdout
+    assert "Number of matches: 36742" in res.read_text()
+    lines = (tmp_path / "run.log.matches").read_text().splitlines()
+    assert int(lines[0]) == 36742
+    got = np.array([[int(x) for x in ln.split()] for ln in lines[1:]], np.uint32)
+    g = graphs("ca_netscience")
+    want = oracle.canonical_instances(oracle.list_embeddings(g.offsets, g.nbrs, p.k, p.edges),
+                                      np.array(sge_perms(sge, p)))
+    assert np.array_equal(got, want)
