@@ -150,7 +150,7 @@ def run_reference(args):
     plans, names = make_plans(sge, st)
     threads = os.cpu_count() or 1
     # bounded sample: every stride-th root; stride sized for ~10-20 s per step
-    stride = int(os.environ.get("SGE_REF_STRIDE", "64"))
+    stride = int(os.environ.get("SGE_REF_STRIDE", "8"))
     def step(offset):
         t0 = time.perf_counter()
         total = 0

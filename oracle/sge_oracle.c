@@ -371,20 +371,86 @@ static uint32_t level_candidates(const exec_ctx *c, uint32_t i, const uint32_t *
     return w;
 }
 
-/* Leaf count (traverse, matching/join.cpp:1520-1691). */
-static uint64_t tail_count(const exec_ctx *c, const uint32_t *mm, uint32_t **bufs, uint32_t *tmp) {
+/* A tail level whose parents all precede the last enumerated level has a
+ * candidate set that does not change while the last levels vary: like a bag
+ * relation built once per binding of its prefix (nodeJoin + buildTrie,
+ * matching/join.cpp:309-421,1713-1717), its intersection is computed when its
+ * last parent is matched and reused (bounds and exclusions applied at the leaf). */
+static int hoisted_level(const sge_plan_blob *p, uint32_t i) {
+    const uint32_t par = p->parents[i];
+    if (i < p->num_enum || __builtin_popcount(par) < 2) return 0;
+    const uint32_t last = 31u - (uint32_t)__builtin_clz(par);
+    return last + 1 < p->num_enum;
+}
+static uint32_t hoist_at_level(const sge_plan_blob *p, uint32_t i) {
+    const uint32_t last = 31u - (uint32_t)__builtin_clz(p->parents[i]);
+    return last < 1 ? 1u : last;
+}
+
+/* Intersection of the parents' lists of level i, no bounds, no exclusions. */
+static uint32_t raw_intersection(const exec_ctx *c, uint32_t i, const uint32_t *mm, uint32_t *out, uint32_t *tmp) {
+    const sge_plan_blob *p = c->p;
+    const uint32_t *lists[32];
+    uint32_t lens[32], nl = 0;
+    for (uint32_t msk = p->parents[i]; msk; msk &= msk - 1) {
+        uint32_t v = mm[__builtin_ctz(msk)];
+        lists[nl] = c->nb + c->off[v];
+        lens[nl] = c->off[v + 1] - c->off[v];
+        ++nl;
+    }
+    for (uint32_t x = 0; x < nl; ++x)
+        for (uint32_t y = x + 1; y < nl; ++y)
+            if (lens[y] < lens[x]) {
+                const uint32_t *t = lists[x]; lists[x] = lists[y]; lists[y] = t;
+                uint32_t tl = lens[x]; lens[x] = lens[y]; lens[y] = tl;
+            }
+    uint32_t n = lens[0];
+    memcpy(out, lists[0], sizeof(uint32_t) * n);
+    for (uint32_t l = 1; l < nl && n; ++l) {
+        n = oracle_intersect(out, n, lists[l], lens[l], tmp);
+        memcpy(out, tmp, sizeof(uint32_t) * n);
+    }
+    return n;
+}
+
+/* Level i's candidates from a stored hoisted list: bound trim (setBeginPos /
+ * setEndPos) and the matched vertices dropped (visited[]). */
+static uint32_t from_hoisted(const exec_ctx *c, uint32_t i, const uint32_t *mm, const uint32_t *h, uint32_t hn,
+                             uint32_t *out) {
+    const sge_plan_blob *p = c->p;
+    uint32_t lo = 0, hi = 0xFFFFFFFFu;
+    for (uint32_t msk = p->lower[i]; msk; msk &= msk - 1) if (mm[__builtin_ctz(msk)] > lo) lo = mm[__builtin_ctz(msk)];
+    for (uint32_t msk = p->upper[i]; msk; msk &= msk - 1) if (mm[__builtin_ctz(msk)] < hi) hi = mm[__builtin_ctz(msk)];
+    uint32_t b = p->lower[i] ? oracle_set_begin_pos(h, hn, lo) : 0;
+    uint32_t e = p->upper[i] ? oracle_set_end_pos(h, hn, hi) : hn;
+    uint32_t w = 0;
+    for (uint32_t x = b; x < e; ++x) {
+        int ex = 0;
+        for (uint32_t msk = p->check[i]; msk; msk &= msk - 1) if (mm[__builtin_ctz(msk)] == h[x]) ex = 1;
+        if (!ex) out[w++] = h[x];
+    }
+    return w;
+}
+
+/* Leaf count (traverse, matching/join.cpp:1520-1691).  hoist[i]/hoist_n[i]
+ * hold the stored list of hoisted tail levels (NULL otherwise). */
+static uint64_t tail_count(const exec_ctx *c, const uint32_t *mm, uint32_t **bufs, uint32_t *tmp,
+                           uint32_t *const *hoist, const uint32_t *hoist_n) {
     const sge_plan_blob *p = c->p;
     const uint32_t ne = p->num_enum, T = p->tail_len;
+    #define TAIL_CANDS(i, out) (hoist[(i)] ? from_hoisted(c, (i), mm, hoist[(i)], hoist_n[(i)], (out)) \
+                                           : level_candidates(c, (i), mm, (out), tmp))
     if (p->tail_mode == SGE_TAIL_SINGLE || p->tail_mode == SGE_TAIL_CHOOSE) {
-        uint32_t n = level_candidates(c, ne, mm, bufs[0], tmp);
+        uint32_t n = TAIL_CANDS(ne, bufs[0]);
         return p->tail_mode == SGE_TAIL_SINGLE ? (uint64_t)n : oracle_binom_exact(n, (int)T);
     }
     const uint32_t *sets[SGE_MAX_TAIL];
     uint32_t lens[SGE_MAX_TAIL];
     for (uint32_t t = 0; t < T; ++t) {
-        lens[t] = level_candidates(c, ne + t, mm, bufs[t], tmp);
+        lens[t] = TAIL_CANDS(ne + t, bufs[t]);
         sets[t] = bufs[t];
     }
+    #undef TAIL_CANDS
     return oracle_num_unique_combine(sets, lens, (int)T);
 }
 
@@ -415,6 +481,13 @@ uint64_t oracle_count_plan(const uint32_t *off, const uint32_t *nb, uint32_t n, 
         for (uint32_t i = 0; i < SGE_MAX_K + SGE_MAX_TAIL; ++i) bufs[i] = (uint32_t *)malloc(sizeof(uint32_t) * (c.maxdeg + 1));
         uint32_t *tmp = (uint32_t *)malloc(sizeof(uint32_t) * (c.maxdeg + 1));
         uint32_t cnt[SGE_MAX_K], it[SGE_MAX_K], mm[SGE_MAX_K];
+        uint32_t *hoist[SGE_MAX_K], hoist_n[SGE_MAX_K];
+        for (uint32_t i = 0; i < SGE_MAX_K; ++i) {
+            hoist[i] = NULL;
+            hoist_n[i] = 0;
+        }
+        for (uint32_t i = ne; i < K; ++i)
+            if (hoisted_level(p, i)) hoist[i] = (uint32_t *)malloc(sizeof(uint32_t) * (c.maxdeg + 1));
         (void)K;
 #ifdef _OPENMP
 #pragma omp for schedule(dynamic, 64)
@@ -426,20 +499,25 @@ uint64_t oracle_count_plan(const uint32_t *off, const uint32_t *nb, uint32_t n, 
             else { a = eu[t]; b = ev[t]; if (p->root_kind == SGE_ROOT_DESC) { uint32_t x = a; a = b; b = x; } }
             mm[0] = a; mm[1] = b;
             ++done;
-            if (ne == 2) { total += tail_count(&c, mm, bufs + SGE_MAX_K, tmp); continue; }
+            if (ne == 2) { total += tail_count(&c, mm, bufs + SGE_MAX_K, tmp, hoist, hoist_n); continue; }
+            for (uint32_t i = ne; i < K; ++i)
+                if (hoist[i] && hoist_at_level(p, i) == 1) hoist_n[i] = raw_intersection(&c, i, mm, hoist[i], tmp);
             int lv = 2;
             cnt[2] = level_candidates(&c, 2, mm, bufs[2], tmp);
             it[2] = 0;
             while (lv >= 2) {
                 if (it[lv] >= cnt[lv]) { --lv; continue; }
                 mm[lv] = bufs[lv][it[lv]++];
-                if ((uint32_t)lv + 1 == ne) { total += tail_count(&c, mm, bufs + SGE_MAX_K, tmp); continue; }
+                for (uint32_t i = ne; i < K; ++i)
+                    if (hoist[i] && hoist_at_level(p, i) == (uint32_t)lv) hoist_n[i] = raw_intersection(&c, i, mm, hoist[i], tmp);
+                if ((uint32_t)lv + 1 == ne) { total += tail_count(&c, mm, bufs + SGE_MAX_K, tmp, hoist, hoist_n); continue; }
                 ++lv;
                 cnt[lv] = level_candidates(&c, (uint32_t)lv, mm, bufs[lv], tmp);
                 it[lv] = 0;
             }
         }
         for (uint32_t i = 0; i < SGE_MAX_K + SGE_MAX_TAIL; ++i) free(bufs[i]);
+        for (uint32_t i = 0; i < SGE_MAX_K; ++i) free(hoist[i]);
         free(tmp);
     }
     free(eu);

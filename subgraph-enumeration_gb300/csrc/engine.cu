@@ -49,14 +49,19 @@ struct DevGraph {
 
 // Compact device form of sge_plan_blob (+ batch bookkeeping).
 struct DevPlan {
-    uint32_t parents[SGE_MAX_K], lower[SGE_MAX_K], upper[SGE_MAX_K], check[SGE_MAX_K], rest[SGE_MAX_K];
-    int32_t base[SGE_MAX_K];
-    uint32_t after[SGE_MAX_K];       // exploration: later levels having this level as a parent
+    // level masks fit 16 bits (k <= SGE_MAX_K = 16); small fields are bytes,
+    // which keeps the per-warp shared-memory copy of the plan small
+    uint16_t parents[SGE_MAX_K], lower[SGE_MAX_K], upper[SGE_MAX_K], check[SGE_MAX_K], rest[SGE_MAX_K];
+    uint16_t after[SGE_MAX_K];          // exploration: later levels having this level as a parent
+    int8_t base[SGE_MAX_K];
+    uint8_t order_[SGE_MAX_K];          // pattern vertex of each level (enumeration output order)
+    uint8_t hoist_at[SGE_MAX_K];        // level after whose match a hoisted list is computed
     int8_t slot[SGE_MAX_K][SGE_MAX_K];  // exploration: buffer slot of version (j, i), -1 = direct N(m[j])
+    int8_t part_coef[SGE_MAX_PARTITIONS];
+    uint8_t part_nblocks[SGE_MAX_PARTITIONS];
+    uint8_t part_block[SGE_MAX_PARTITIONS][SGE_MAX_TAIL];
+    uint8_t pad_[2];
     uint32_t k, ne, T, tail_mode, join_style, root_kind, nparts, nbufs;
-    int32_t part_coef[SGE_MAX_PARTITIONS];
-    uint32_t part_nblocks[SGE_MAX_PARTITIONS];
-    uint32_t part_block[SGE_MAX_PARTITIONS][SGE_MAX_TAIL];
     unsigned long long task_begin, ntasks;        // this batch's task range for the plan
     unsigned long long root_stride, root_offset;  // task j of the plan = root root_offset + j*root_stride
     unsigned long long mult;                      // count multiplier (|Aut| for single-bag plans)
@@ -68,9 +73,8 @@ struct DevPlan {
     uint32_t split_H;                             // roots whose level-2 bound exceeds this are deferred
     uint32_t split_S;                             // level-2 candidates per deferred task (0 = never defer)
     uint32_t split_C;                             // deferred tasks per heavy root (max degree / S, rounded up)
-    uint32_t order_[SGE_MAX_K];                   // pattern vertex of each level (enumeration output order)
-    uint32_t hoist_at[SGE_MAX_K];                 // level after whose match a hoisted list is computed
 };
+static_assert(sizeof(DevPlan) % 4 == 0, "DevPlan is copied as 32-bit words");
 
 struct DevStats {
     unsigned long long set_ops, alg_bytes, partial, roots;
@@ -644,7 +648,9 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
         int bsrc = -2;
         // a tail level with a single list (after reuse) is counted without a
         // scan: range size minus the matched vertices inside it (numResults)
-        const bool direct = P.tail_mode != SGE_TAIL_IEP && tail_list_count(P, W, L, c, lc, 0, i) == 1;
+        // (the last inclusion–exclusion pass probes no other tail level, so it
+        // is a plain count too)
+        const bool direct = (P.tail_mode != SGE_TAIL_IEP || t + 1 == T) && tail_list_count(P, W, L, c, lc, 0, i) == 1;
         if (direct) {
             if (lane < ncand) {
                 for_tail_lists(P, W, L, c, lc, lane, i, [&](const uint32_t *p, uint32_t len, int, bool) {
@@ -660,7 +666,8 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
                     if ((!b.has_lo || v > b.lo) && (!b.has_hi || v < b.hi) && contains(bp, blen, v)) --cnt;
                 }
                 if (P.tail_mode == SGE_TAIL_SINGLE) single += cnt;
-                else L.cnt[lane][1] = cnt;
+                else if (P.tail_mode == SGE_TAIL_CHOOSE) L.cnt[lane][1] = cnt;
+                else L.cnt[lane][1u << t] = cnt;
                 if (STATS) bytes += 4ull * (2u + __popc(P.check[i])) * (31u - __clz(blen + 1u));
             }
             __syncwarp();
@@ -867,16 +874,20 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
     return ok ? acc : 0ull;
 }
 
-// Per-warp shared-memory carve-up: WarpState | LeafState | 3 tables.
+// Per-warp shared-memory carve-up: DevPlan | WarpState | LeafState | 3 tables.
 __host__ __device__ constexpr size_t align128(size_t x) { return (x + 127) & ~(size_t)127; }
 __host__ __device__ inline size_t warp_smem_bytes(uint32_t tw) {
-    return align128(sizeof(WarpState)) + align128(sizeof(LeafState)) + align128(3ull * tw * sizeof(uint32_t));
+    return align128(sizeof(DevPlan)) + align128(sizeof(WarpState)) + align128(sizeof(LeafState)) +
+           align128(3ull * tw * sizeof(uint32_t));
+}
+__device__ __forceinline__ DevPlan &warp_plan(unsigned char *smem, uint32_t wib, uint32_t tw) {
+    return *reinterpret_cast<DevPlan *>(smem + (size_t)wib * warp_smem_bytes(tw));
 }
 
 template <bool STATS>
 __device__ __forceinline__ WarpState &setup_warp(unsigned char *smem, uint32_t wib, uint32_t tw, uint32_t tmode,
                                                  Ctx<STATS> &c) {
-    unsigned char *base = smem + (size_t)wib * warp_smem_bytes(tw);
+    unsigned char *base = smem + (size_t)wib * warp_smem_bytes(tw) + align128(sizeof(DevPlan));
     WarpState &W = *reinterpret_cast<WarpState *>(base);
     c.L = reinterpret_cast<LeafState *>(base + align128(sizeof(WarpState)));
     c.tab = reinterpret_cast<uint32_t *>(base + align128(sizeof(WarpState)) + align128(sizeof(LeafState)));
@@ -926,8 +937,7 @@ __global__ void __launch_bounds__(256, 3) count_kernel(DevGraph g, const DevPlan
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t lane = lane_id();
     const uint32_t wib = threadIdx.x >> 5;
-    __shared__ DevPlan Psh[8];
-    DevPlan &P = Psh[wib];
+    DevPlan &P = warp_plan(smem_raw, wib, tw);
     const size_t gwarp = (size_t)blockIdx.x * (blockDim.x >> 5) + wib;
     Ctx<STATS> c;
     c.g = g;
@@ -1027,8 +1037,7 @@ __global__ void __launch_bounds__(256) enum_kernel(DevGraph g, const DevPlan *__
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t lane = lane_id();
     const uint32_t wib = threadIdx.x >> 5;
-    __shared__ DevPlan Psh[8];
-    DevPlan &P = Psh[wib];
+    DevPlan &P = warp_plan(smem_raw, wib, 0u);
     const size_t gwarp = (size_t)blockIdx.x * (blockDim.x >> 5) + wib;
     Ctx<false> c;
     c.g = g;
@@ -1155,12 +1164,12 @@ namespace {
 void to_devplan(const sge_plan_blob &b, DevPlan &d) {
     memset(&d, 0, sizeof d);
     for (uint32_t i = 0; i < SGE_MAX_K; ++i) {
-        d.parents[i] = b.parents[i];
-        d.lower[i] = b.lower[i];
-        d.upper[i] = b.upper[i];
-        d.check[i] = b.check[i];
-        d.rest[i] = b.rest[i];
-        d.base[i] = b.base[i];
+        d.parents[i] = (uint16_t)b.parents[i];
+        d.lower[i] = (uint16_t)b.lower[i];
+        d.upper[i] = (uint16_t)b.upper[i];
+        d.check[i] = (uint16_t)b.check[i];
+        d.rest[i] = (uint16_t)b.rest[i];
+        d.base[i] = (int8_t)b.base[i];
         for (uint32_t j = 0; j < SGE_MAX_K; ++j) d.slot[i][j] = -1;
     }
     d.k = b.k;
@@ -1171,9 +1180,9 @@ void to_devplan(const sge_plan_blob &b, DevPlan &d) {
     d.root_kind = b.root_kind;
     d.nparts = b.num_partitions;
     for (uint32_t p = 0; p < SGE_MAX_PARTITIONS; ++p) {
-        d.part_coef[p] = b.part_coef[p];
-        d.part_nblocks[p] = b.part_nblocks[p];
-        for (uint32_t x = 0; x < SGE_MAX_TAIL; ++x) d.part_block[p][x] = b.part_block[p][x];
+        d.part_coef[p] = (int8_t)b.part_coef[p];
+        d.part_nblocks[p] = (uint8_t)b.part_nblocks[p];
+        for (uint32_t x = 0; x < SGE_MAX_TAIL; ++x) d.part_block[p][x] = (uint8_t)b.part_block[p][x];
     }
     uint32_t nb = 0;
     if (b.join_style == SGE_JOIN_EXPLORATION) {
@@ -1182,7 +1191,7 @@ void to_devplan(const sge_plan_blob &b, DevPlan &d) {
             bool first = true;
             for (uint32_t msk = par; msk; msk &= msk - 1) {
                 uint32_t j = (uint32_t)__builtin_ctz(msk);
-                d.after[j] |= 1u << i;
+                d.after[j] = (uint16_t)(d.after[j] | (1u << i));
                 if (first) { d.slot[j][i] = -1; first = false; }
                 else d.slot[j][i] = (int8_t)nb++;
             }
@@ -1210,13 +1219,13 @@ void to_devplan(const sge_plan_blob &b, DevPlan &d) {
             const uint32_t last = 31u - (uint32_t)__builtin_clz(par);
             if (__builtin_popcount(par) >= 2 && last + 1 < b.num_enum) {
                 d.hoist_mask |= 1u << i;
-                d.hoist_at[i] = last < 1 ? 1u : last;
+                d.hoist_at[i] = (uint8_t)(last < 1 ? 1u : last);
             }
         }
     d.mult = b.count_multiplier;
     d.chunk = 1;
     d.split_par = b.num_enum >= 3 ? (b.parents[2] & 3u) : 0u;
-    for (uint32_t i = 0; i < SGE_MAX_K; ++i) d.order_[i] = b.order[i];
+    for (uint32_t i = 0; i < SGE_MAX_K; ++i) d.order_[i] = (uint8_t)b.order[i];
     d.split_S = 0;  // set per graph in sge_count
 }
 
@@ -1330,19 +1339,35 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
         L.nbufs = std::max(L.nbufs, d.nbufs);
         if (d.k > SGE_MAX_K) return fail(SGE_UNSUPPORTED, "plan %u has k=%u", i, d.k);
     }
-    L.wpb = o.warps_per_block ? std::min<uint32_t>(o.warps_per_block, 8) : 8;
-    L.threads = L.wpb * 32;
     // pinned-list tables: a bitmap over all vertices when it fits in 4 KB, else a 512-slot hash
     if (g->n <= 32768u) { L.tmode = 1; L.tw = std::max<uint32_t>(32u, ((g->n + 31u) / 32u + 31u) & ~31u); }
     else { L.tmode = 2; L.tw = 512; }
-    L.smem = warp_smem_bytes(L.tw) * L.wpb;
     L.want_stats = o.collect_counters != 0;
+    // warps per block: 8 or 4, whichever keeps more warps resident per SM
+    // (shared memory per warp is several KB, so smaller blocks pack better)
     int bps = 0;
-    // static (plan copies) + dynamic shared memory exceed the 48 KB default: opt in
-    CUDA_TRY(cudaFuncSetAttribute(count_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
-    CUDA_TRY(cudaFuncSetAttribute(count_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
-    if (L.want_stats) CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, count_kernel<true>, L.threads, L.smem));
-    else CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, count_kernel<false>, L.threads, L.smem));
+    {
+        int best_warps = -1;
+        const uint32_t choices[2] = {8, 4};
+        for (uint32_t wpb : choices) {
+            if (o.warps_per_block && wpb != std::min<uint32_t>(o.warps_per_block, 8)) continue;
+            const size_t smem = warp_smem_bytes(L.tw) * wpb;
+            int b = 0;
+            // static (plan copies) + dynamic shared memory exceed the 48 KB default: opt in
+            CUDA_TRY(cudaFuncSetAttribute(count_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            CUDA_TRY(cudaFuncSetAttribute(count_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            if (L.want_stats) CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, count_kernel<true>, wpb * 32, smem));
+            else CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, count_kernel<false>, wpb * 32, smem));
+            if (b * (int)wpb > best_warps) { best_warps = b * (int)wpb; bps = b; L.wpb = wpb; L.smem = smem; }
+        }
+        if (o.warps_per_block && best_warps < 0) {
+            L.wpb = std::min<uint32_t>(std::max<uint32_t>(o.warps_per_block, 1), 8);
+            L.smem = warp_smem_bytes(L.tw) * L.wpb;
+        }
+        L.threads = L.wpb * 32;
+        CUDA_TRY(cudaFuncSetAttribute(count_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
+        CUDA_TRY(cudaFuncSetAttribute(count_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
+    }
     if (o.blocks_per_sm) bps = std::min<int>(bps, (int)o.blocks_per_sm);
     bps = std::max(bps, 1);
     L.cap = o.max_level_capacity ? o.max_level_capacity : std::max<uint32_t>(g->max_deg, 1);
@@ -1758,8 +1783,7 @@ __global__ void __launch_bounds__(256) count_kernel_noalloc(DevGraph g, const De
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t lane = lane_id();
     const uint32_t wib = threadIdx.x >> 5;
-    __shared__ DevPlan Psh[8];
-    DevPlan &P = Psh[wib];
+    DevPlan &P = warp_plan(smem_raw, wib, 0u);
     const size_t gwarp = (size_t)blockIdx.x * (blockDim.x >> 5) + wib;
     Ctx<false> c;
     c.g = g;
