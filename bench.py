@@ -205,17 +205,20 @@ def cpu_sample(oracle, g, plans, stride, offset, threads):
 
 def cpu_baseline(sge, g, plans, budget_s=15.0):
     """The oracle port on all host cores over the same root sample of every
-    plan of the step (every stride-th root edge), stride sized for ~budget_s."""
+    plan of the step (every stride-th root edge), the stride shrunk until the
+    sample takes about budget_s/3 .. budget_s seconds."""
     sys.path.insert(0, str(REPO / "oracle"))
     import oracle
     threads = os.cpu_count() or 1
-    stride = 8192
-    total, dt, roots = cpu_sample(oracle, g, plans, stride, 7, threads)
-    if dt < budget_s / 4:
-        stride = max(1, int(stride * dt / budget_s) or 1)
+    stride = 1 << 14
+    while True:
         total, dt, roots = cpu_sample(oracle, g, plans, stride, 7 % stride, threads)
+        if dt >= budget_s / 3 or stride == 1:
+            break
+        # aim at budget_s/2, never shrinking the stride by more than 16x per step
+        stride = max(1, stride // max(2, min(16, int(budget_s / 2 / max(dt, 1e-3)))))
     return {"value": total / dt, "unit": "embeddings/s", "cores": threads, "kind": "port",
-            "sample": f"root edges t = 7 mod {stride} of all {len(plans)} plans of a step ({roots} roots, "
+            "sample": f"root edges t = {7 % stride} mod {stride} of all {len(plans)} plans of a step ({roots} roots, "
                       f"{dt:.1f} s); value = embeddings of the sample / its time"}
 
 

@@ -96,6 +96,7 @@ struct WarpState {
     uint32_t vlen[SGE_MAX_K][SGE_MAX_K];  // exploration version lengths (j, i)
     uint32_t pmode[3];                    // pinned N(m[0]), N(m[1]), level-2 list: 0 none, 1 bitmap, 2 hash
     uint32_t hcnt[SGE_MAX_K];             // hoisted tail lists (buffer slot = level)
+    uint32_t hpin;                        // tail level whose hoisted list is pinned in table 2 (0 = none)
 };
 
 // Leaf state (shared memory): up to 32 candidates of the last enumerated
@@ -290,7 +291,13 @@ template <bool STATS>
 __device__ void unpin_root(const DevPlan &P, WarpState &W, Ctx<STATS> &c) {
     for (uint32_t j = 0; j < 2; ++j)
         if (W.pmode[j]) unpin_list(W, c, j, W.lptr[j], W.llen[j]);
-    if (W.pmode[2]) unpin_list(W, c, 2, W.flist[2], W.fcnt[2]);
+    if (W.pmode[2]) {
+        if (W.hpin) unpin_list(W, c, 2, c.buf + (size_t)W.hpin * c.cap, W.hcnt[W.hpin]);
+        else unpin_list(W, c, 2, W.flist[2], W.fcnt[2]);
+    }
+    __syncwarp();
+    if (lane_id() == 0) W.hpin = 0;
+    __syncwarp();
 }
 
 __device__ __forceinline__ void set_match(const DevGraph &g, WarpState &W, uint32_t lv, uint32_t x) {
@@ -434,6 +441,14 @@ __device__ __forceinline__ bool hoist_after(const DevPlan &P, WarpState &W, Ctx<
             if (lane_id() == 0) atomicOr(c.flags, FLAG_OVERFLOW);
             return false;
         }
+        // a list hoisted once per root is probed for every candidate below it:
+        // pin it in the third table when that table is free
+        if (j == 1 && c.tmode && !((P.pin_mask >> 2) & 1u) && W.hpin == 0u && W.pmode[2] == 0u) {
+            pin_list(W, c, 2, out, n);
+            __syncwarp();
+            if (lane_id() == 0 && W.pmode[2]) W.hpin = i;
+            __syncwarp();
+        }
     }
     return true;
 }
@@ -560,7 +575,7 @@ __device__ __forceinline__ void for_tail_lists(const DevPlan &P, const WarpState
     const uint32_t below = (1u << lc.L0) - 1u;
     uint32_t shared = P.parents[i] & below, cand = P.parents[i] & ~below;
     if (!lc.explore && ((P.hoist_mask >> i) & 1u)) {
-        f(c.buf + (size_t)i * c.cap, W.hcnt[i], SRC_HOISTED, false);
+        f(c.buf + (size_t)i * c.cap, W.hcnt[i], SRC_HOISTED, W.hpin == i);
         return;
     }
     if (lc.explore && shared) {
@@ -606,7 +621,7 @@ template <bool STATS>
 __device__ __forceinline__ bool in_list(const WarpState &W, const Ctx<STATS> &c, const uint32_t *p, uint32_t len,
                                         int src, bool pinned, uint32_t y) {
     if (pinned) {
-        const uint32_t ti = src == SRC_LEVEL2_LIST ? 2u : (uint32_t)src;
+        const uint32_t ti = (src == SRC_LEVEL2_LIST || src == SRC_HOISTED) ? 2u : (uint32_t)src;
         return pin_has(c.tab + ti * c.tw, W.pmode[ti], c.tw, y);
     }
     return contains(p, len, y);
@@ -870,7 +885,7 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
         if (lane == 0) W.pos[lv] = 0;
         __syncwarp();
     }
-    if (P.pin_mask) unpin_root(P, W, c);
+    if (P.pin_mask || W.hpin) unpin_root(P, W, c);
     return ok ? acc : 0ull;
 }
 
@@ -895,7 +910,7 @@ __device__ __forceinline__ WarpState &setup_warp(unsigned char *smem, uint32_t w
     c.tmode = tmode;
     const uint32_t fill = tmode == 2 ? PIN_EMPTY : 0u;
     for (uint32_t w = lane_id(); w < 3 * tw; w += 32) c.tab[w] = fill;
-    if (lane_id() == 0) { W.pmode[0] = 0; W.pmode[1] = 0; W.pmode[2] = 0; }
+    if (lane_id() == 0) { W.pmode[0] = 0; W.pmode[1] = 0; W.pmode[2] = 0; W.hpin = 0; }
     __syncwarp();
     return W;
 }
