@@ -149,6 +149,8 @@ typedef struct sge_count_opts {
     uint64_t root_stride;       /* 0/1 = every root task; s > 1: only tasks t ≡ root_offset (mod s) */
     uint64_t root_offset;       /* (root-range sharding across ranks, or sampled runs) */
     uint32_t collect_counters;  /* 1: run the instrumented kernel (set_ops, alg_bytes, partial matches) */
+    uint32_t heavy_threshold;   /* 0 = auto; otherwise roots whose level-2 list may exceed it are split
+                                   into tasks of 128 level-2 candidates run by a second launch */
 } sge_count_opts;
 
 /* Statistics of one sge_count call (per call, summed over plans).  kernel_ms,

@@ -73,6 +73,8 @@ struct DevPlan {
     uint32_t split_H;                             // roots whose level-2 bound exceeds this are deferred
     uint32_t split_S;                             // level-2 candidates per deferred task (0 = never defer)
     uint32_t split_C;                             // deferred tasks per heavy root (max degree / S, rounded up)
+    uint32_t pair;                                // 1: the last two enumerated levels run as one flattened step
+    uint32_t tail_par;                            // union of the tail levels' parents
 };
 static_assert(sizeof(DevPlan) % 4 == 0, "DevPlan is copied as 32-bit words");
 
@@ -99,9 +101,23 @@ struct WarpState {
     uint32_t hpin;                        // tail level whose hoisted list is pinned in table 2 (0 = none)
 };
 
+// One tail level's candidate set as the leaf probes it: its lists (a pinned
+// table, a sorted list, or the CSR list of a candidate's own level = slot),
+// the bound and exclusion values from the levels below the leaf's first
+// candidate level, and which slots add bounds or exclusions.
+struct TailDesc {
+    const uint32_t *ptr[SGE_MAX_K];
+    uint32_t len[SGE_MAX_K];
+    uint32_t exv[SGE_MAX_K];
+    uint32_t lo, hi;
+    uint8_t kind[SGE_MAX_K];  // 0..2 pinned table; 3 sorted list; 4/5 CSR list of slot 0/1
+    uint8_t nsrc, nex, has_lo, has_hi, lo_slots, hi_slots, ex_slots, pad;
+};
+
 // Leaf state (shared memory): up to 32 candidates of the last enumerated
 // level, each with its own matched values for the levels from L0 on.
 struct LeafState {
+    TailDesc td[SGE_MAX_TAIL];
     uint32_t cm[32][2];
     const uint32_t *cptr[32][2];
     uint32_t clen[32][2];
@@ -110,6 +126,27 @@ struct LeafState {
     int32_t bsrc[32];
     uint32_t pref[32];
     uint32_t cnt[32][16];
+};
+
+// Pair step (shared memory): level a = ne-2 of the DFS is processed 32
+// candidates x at a time; level a+1's candidates y of all 32 are generated in
+// one flattened scan, and the (x, y) pairs go to the leaf 32 at a time.
+struct PairState {
+    const uint32_t *sptr[SGE_MAX_K];  // level a+1's lists that do not depend on x
+    uint32_t slen[SGE_MAX_K];
+    int32_t stab[SGE_MAX_K];          // pinned table holding the list, -1 = none
+    uint32_t ns;                      // number of such lists
+    uint32_t xpar;                    // 1: N(x) is also one of level a+1's lists
+    uint32_t exv[SGE_MAX_K];          // matched values below a that level a+1 excludes
+    uint32_t nex;
+    uint32_t x[32];                   // this batch's level-a candidates
+    const uint32_t *xp[32];           // N(x)
+    uint32_t xl[32];
+    const uint32_t *bp[32];           // list scanned for candidate x (trimmed by bounds)
+    uint32_t bl[32];
+    int32_t bs[32];                   // scanned list: index into sptr, or -1 for N(x)
+    uint32_t pref[32];
+    uint32_t qx[64], qy[64];          // (x, y) pairs waiting for the leaf
 };
 
 constexpr uint32_t PIN_EMPTY = 0xFFFFFFFFu;
@@ -206,6 +243,7 @@ struct Ctx {
     uint32_t tw;
     uint32_t tmode;   // 0 none, 1 bitmap over all vertices, 2 open-addressing hash
     LeafState *L;
+    PairState *PS;
     unsigned long long tstart, deadline;  // globaltimer of the warp's start; budget in ns (0 = none)
     unsigned long long set_ops, alg_bytes, partial;
 };
@@ -542,30 +580,6 @@ struct LeafCtx {
     bool explore;  // exploration: shared parents of a tail level are one running list
 };
 
-__device__ __forceinline__ uint32_t cand_val(const WarpState &W, const LeafState &L, const LeafCtx &lc, uint32_t l,
-                                             uint32_t p) {
-    return p >= lc.L0 ? L.cm[l][p - lc.L0] : W.m[p];
-}
-
-__device__ __forceinline__ Bounds cand_bounds(const DevPlan &P, const WarpState &W, const LeafState &L,
-                                              const LeafCtx &lc, uint32_t l, uint32_t i) {
-    Bounds b;
-    b.lo = 0;
-    b.hi = 0xFFFFFFFFu;
-    b.has_lo = P.lower[i] != 0;
-    b.has_hi = P.upper[i] != 0;
-    for (uint32_t msk = P.lower[i]; msk; msk &= msk - 1) b.lo = max(b.lo, cand_val(W, L, lc, l, __ffs(msk) - 1));
-    for (uint32_t msk = P.upper[i]; msk; msk &= msk - 1) b.hi = min(b.hi, cand_val(W, L, lc, l, __ffs(msk) - 1));
-    return b;
-}
-
-__device__ __forceinline__ bool cand_excluded(const DevPlan &P, const WarpState &W, const LeafState &L,
-                                              const LeafCtx &lc, uint32_t l, uint32_t i, uint32_t y) {
-    bool ex = false;
-    for (uint32_t msk = P.check[i]; msk; msk &= msk - 1) ex |= (cand_val(W, L, lc, l, __ffs(msk) - 1) == y);
-    return ex;
-}
-
 // Visits the lists whose intersection is tail level i's candidate set for
 // candidate l: f(ptr, len, src, pinned) with src = level of the list, or -1 for
 // the shared running list (exploration).  f returns false to stop.
@@ -609,37 +623,98 @@ __device__ __forceinline__ void for_tail_lists(const DevPlan &P, const WarpState
     }
 }
 
-template <bool STATS>
-__device__ __forceinline__ uint32_t tail_list_count(const DevPlan &P, const WarpState &W, const LeafState &L,
-                                                    const Ctx<STATS> &c, const LeafCtx &lc, uint32_t l, uint32_t i) {
-    uint32_t n = 0;
-    for_tail_lists(P, W, L, c, lc, l, i, [&](const uint32_t *, uint32_t, int, bool) { ++n; return true; });
-    return n;
+// Lists, bounds and exclusions of one tail level, described once per leaf
+// call: the same for every candidate except the lists of the candidates' own
+// levels (slots), which are looked up per candidate.
+__device__ __forceinline__ Bounds td_bounds(const TailDesc &D, const LeafState &L, uint32_t l) {
+    Bounds b;
+    b.lo = D.lo;
+    b.hi = D.hi;
+    b.has_lo = D.has_lo;
+    b.has_hi = D.has_hi;
+    if (D.lo_slots & 1u) b.lo = max(b.lo, L.cm[l][0]);
+    if (D.lo_slots & 2u) b.lo = max(b.lo, L.cm[l][1]);
+    if (D.hi_slots & 1u) b.hi = min(b.hi, L.cm[l][0]);
+    if (D.hi_slots & 2u) b.hi = min(b.hi, L.cm[l][1]);
+    return b;
 }
 
-template <bool STATS>
-__device__ __forceinline__ bool in_list(const WarpState &W, const Ctx<STATS> &c, const uint32_t *p, uint32_t len,
-                                        int src, bool pinned, uint32_t y) {
-    if (pinned) {
-        const uint32_t ti = (src == SRC_LEVEL2_LIST || src == SRC_HOISTED) ? 2u : (uint32_t)src;
-        return pin_has(c.tab + ti * c.tw, W.pmode[ti], c.tw, y);
-    }
-    return contains(p, len, y);
+__device__ __forceinline__ const uint32_t *td_ptr(const TailDesc &D, const LeafState &L, uint32_t q, uint32_t l) {
+    return D.kind[q] >= 4 ? L.cptr[l][D.kind[q] - 4] : D.ptr[q];
+}
+__device__ __forceinline__ uint32_t td_len(const TailDesc &D, const LeafState &L, uint32_t q, uint32_t l) {
+    return D.kind[q] >= 4 ? L.clen[l][D.kind[q] - 4] : D.len[q];
 }
 
-// y ∈ candidates of tail level u for candidate l (bounds, lists, exclusions).
+// y ∈ list q of the level for candidate l.
 template <bool STATS>
-__device__ __forceinline__ bool in_tail_set(const DevPlan &P, const WarpState &W, const LeafState &L,
-                                            const Ctx<STATS> &c, const LeafCtx &lc, uint32_t l, uint32_t u,
-                                            uint32_t y) {
-    Bounds b = cand_bounds(P, W, L, lc, l, u);
+__device__ __forceinline__ bool td_has(const TailDesc &D, const LeafState &L, const WarpState &W,
+                                       const Ctx<STATS> &c, uint32_t q, uint32_t l, uint32_t y) {
+    const uint32_t k = D.kind[q];
+    if (k < 3) return pin_has(c.tab + k * c.tw, W.pmode[k], c.tw, y);
+    if (k == 3) return contains(D.ptr[q], D.len[q], y);
+    return contains(L.cptr[l][k - 4], L.clen[l][k - 4], y);
+}
+
+__device__ __forceinline__ bool td_excluded(const TailDesc &D, const LeafState &L, uint32_t l, uint32_t y) {
+    bool ex = false;
+    for (uint32_t e = 0; e < D.nex; ++e) ex |= D.exv[e] == y;
+    if (D.ex_slots & 1u) ex |= L.cm[l][0] == y;
+    if (D.ex_slots & 2u) ex |= L.cm[l][1] == y;
+    return ex;
+}
+
+// y ∈ the level's candidate set for candidate l (bounds, every list, exclusions).
+template <bool STATS>
+__device__ __forceinline__ bool td_member(const TailDesc &D, const LeafState &L, const WarpState &W,
+                                          const Ctx<STATS> &c, uint32_t l, uint32_t y) {
+    const Bounds b = td_bounds(D, L, l);
     if ((b.has_lo && y <= b.lo) || (b.has_hi && y >= b.hi)) return false;
-    bool ok = true;
-    for_tail_lists(P, W, L, c, lc, l, u, [&](const uint32_t *p, uint32_t len, int src, bool pinned) {
-        ok = in_list(W, c, p, len, src, pinned, y);
-        return ok;
+    for (uint32_t q = 0; q < D.nsrc; ++q)
+        if (!td_has(D, L, W, c, q, l, y)) return false;
+    return !td_excluded(D, L, l, y);
+}
+
+// Fills D for tail level i from the lists for_tail_lists visits.
+template <bool STATS>
+__device__ void tail_desc(const DevPlan &P, const WarpState &W, const LeafState &L, const Ctx<STATS> &c,
+                          const LeafCtx &lc, uint32_t i, TailDesc &D) {
+    uint32_t n = 0;
+    for_tail_lists(P, W, L, c, lc, 0, i, [&](const uint32_t *p, uint32_t len, int src, bool pinned) {
+        uint32_t k = 3;
+        if (pinned) k = (src == SRC_LEVEL2_LIST || src == SRC_HOISTED) ? 2u : (uint32_t)src;
+        else if (src >= (int)lc.L0 && src < SRC_LEVEL2_LIST) k = 4u + (uint32_t)src - lc.L0;
+        D.kind[n] = (uint8_t)k;
+        D.ptr[n] = p;
+        D.len[n] = len;
+        ++n;
+        return true;
     });
-    return ok && !cand_excluded(P, W, L, lc, l, u, y);
+    D.nsrc = (uint8_t)n;
+    D.has_lo = P.lower[i] != 0;
+    D.has_hi = P.upper[i] != 0;
+    uint32_t lo = 0, hi = 0xFFFFFFFFu, los = 0, his = 0, exs = 0, nex = 0;
+    for (uint32_t msk = P.lower[i]; msk; msk &= msk - 1) {
+        const uint32_t q = __ffs(msk) - 1;
+        if (q >= lc.L0) los |= 1u << (q - lc.L0);
+        else lo = max(lo, W.m[q]);
+    }
+    for (uint32_t msk = P.upper[i]; msk; msk &= msk - 1) {
+        const uint32_t q = __ffs(msk) - 1;
+        if (q >= lc.L0) his |= 1u << (q - lc.L0);
+        else hi = min(hi, W.m[q]);
+    }
+    for (uint32_t msk = P.check[i]; msk; msk &= msk - 1) {
+        const uint32_t q = __ffs(msk) - 1;
+        if (q >= lc.L0) exs |= 1u << (q - lc.L0);
+        else D.exv[nex++] = W.m[q];
+    }
+    D.lo = lo;
+    D.hi = hi;
+    D.lo_slots = (uint8_t)los;
+    D.hi_slots = (uint8_t)his;
+    D.ex_slots = (uint8_t)exs;
+    D.nex = (uint8_t)nex;
 }
 
 template <bool STATS>
@@ -650,64 +725,80 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
     const uint32_t ne = P.ne, T = P.T;
     LeafCtx lc{L0, P.join_style == SGE_JOIN_EXPLORATION && L0 > 0};
     const uint32_t passes = (P.tail_mode == SGE_TAIL_IEP) ? T : 1u;
+    // lane t describes tail level ne+t (IEP passes probe the later levels too)
+    __syncwarp();
+    if (lane < passes) tail_desc(P, W, L, c, lc, ne + lane, L.td[lane]);
     if (P.tail_mode != SGE_TAIL_SINGLE) {
 #pragma unroll
         for (uint32_t q = 0; q < 16; ++q) L.cnt[lane][q] = 0;
     }
+    __syncwarp();
+    // inclusion–exclusion: S[A] (A a set of tail positions) is counted in the
+    // pass of A's first position in pass order, probing the later ones; the
+    // sums do not depend on the order, so levels with one list go last (the
+    // last pass is then a plain count and the earlier passes probe them
+    // through a pinned table or one search, not a scan)
+    uint32_t ord = 0;  // 4 bits per pass: tail position
+    if (passes > 1) {
+        uint32_t n = 0;
+        for (uint32_t q = 0; q < passes; ++q)
+            if (L.td[q].nsrc != 1) ord |= q << (4 * n++);
+        for (uint32_t q = 0; q < passes; ++q)
+            if (L.td[q].nsrc == 1) ord |= q << (4 * n++);
+    }
     unsigned long long single = 0, bytes = 0;
     for (uint32_t t = 0; t < passes; ++t) {
-        const uint32_t i = ne + t;
-        // 1. each candidate picks the list it scans (cheapest scan × probes), trimmed by its bounds
-        const uint32_t *bp = nullptr;
-        uint32_t blen = 0;
-        int bsrc = -2;
+        const uint32_t tp = (ord >> (4 * t)) & 15u;
+        const TailDesc &D = L.td[tp];
         // a tail level with a single list (after reuse) is counted without a
         // scan: range size minus the matched vertices inside it (numResults)
         // (the last inclusion–exclusion pass probes no other tail level, so it
         // is a plain count too)
-        const bool direct = (P.tail_mode != SGE_TAIL_IEP || t + 1 == T) && tail_list_count(P, W, L, c, lc, 0, i) == 1;
+        const bool direct = (P.tail_mode != SGE_TAIL_IEP || t + 1 == T) && D.nsrc == 1;
         if (direct) {
             if (lane < ncand) {
-                for_tail_lists(P, W, L, c, lc, lane, i, [&](const uint32_t *p, uint32_t len, int, bool) {
-                    bp = p;
-                    blen = len;
-                    return false;
-                });
-                Bounds b = cand_bounds(P, W, L, lc, lane, i);
+                const uint32_t *fp = td_ptr(D, L, 0, lane);
+                const uint32_t fl = td_len(D, L, 0, lane);
+                const Bounds b = td_bounds(D, L, lane);
+                const uint32_t *bp = fp;
+                uint32_t blen = fl;
                 trim(bp, blen, b);
                 uint32_t cnt = blen;
-                for (uint32_t msk = P.check[i]; msk; msk &= msk - 1) {
-                    const uint32_t v = cand_val(W, L, lc, lane, __ffs(msk) - 1);
-                    if ((!b.has_lo || v > b.lo) && (!b.has_hi || v < b.hi) && contains(bp, blen, v)) --cnt;
-                }
+                auto drop = [&](uint32_t v) {
+                    if ((!b.has_lo || v > b.lo) && (!b.has_hi || v < b.hi) && td_has(D, L, W, c, 0, lane, v)) --cnt;
+                };
+                for (uint32_t e = 0; e < D.nex; ++e) drop(D.exv[e]);
+                if (D.ex_slots & 1u) drop(L.cm[lane][0]);
+                if (D.ex_slots & 2u) drop(L.cm[lane][1]);
                 if (P.tail_mode == SGE_TAIL_SINGLE) single += cnt;
                 else if (P.tail_mode == SGE_TAIL_CHOOSE) L.cnt[lane][1] = cnt;
-                else L.cnt[lane][1u << t] = cnt;
-                if (STATS) bytes += 4ull * (2u + __popc(P.check[i])) * (31u - __clz(blen + 1u));
+                else L.cnt[lane][1u << tp] = cnt;
+                if (STATS) bytes += 4ull * (2u + __popc(P.check[ne + tp])) * (31u - __clz(blen + 1u));
             }
             __syncwarp();
             continue;
         }
+        // 1. each candidate scans its cheapest list (scan length × probes of the others), trimmed by its bounds
+        const uint32_t *bp = nullptr;
+        uint32_t blen = 0, bq = 0;
         if (lane < ncand) {
-            // scan cost of list q = len(q) × (1 + Σ probe costs of the others)
             unsigned long long allp = 0, bestcost = ~0ull;
-            for_tail_lists(P, W, L, c, lc, lane, i, [&](const uint32_t *p, uint32_t len, int src, bool pinned) {
-                allp += pinned ? 1u : 2u + (31u - __clz(len + 1u));
-                return true;
-            });
-            for_tail_lists(P, W, L, c, lc, lane, i, [&](const uint32_t *p, uint32_t len, int src, bool pinned) {
-                unsigned long long own = pinned ? 1u : 2u + (31u - __clz(len + 1u));
-                unsigned long long cost = (unsigned long long)len * (allp - own + 1);
-                if (cost < bestcost) { bestcost = cost; bp = p; blen = len; bsrc = src; }
+            for (uint32_t q = 0; q < D.nsrc; ++q)
+                allp += D.kind[q] < 3 ? 1u : 2u + (31u - __clz(td_len(D, L, q, lane) + 1u));
+            for (uint32_t q = 0; q < D.nsrc; ++q) {
+                const uint32_t len = td_len(D, L, q, lane);
+                const unsigned long long own = D.kind[q] < 3 ? 1u : 2u + (31u - __clz(len + 1u));
+                const unsigned long long cost = (unsigned long long)len * (allp - own + 1);
+                if (cost < bestcost) { bestcost = cost; bq = q; }
                 if (STATS) bytes += 4ull * len;
-                return true;
-            });
-            Bounds b = cand_bounds(P, W, L, lc, lane, i);
-            trim(bp, blen, b);
+            }
+            bp = td_ptr(D, L, bq, lane);
+            blen = td_len(D, L, bq, lane);
+            trim(bp, blen, td_bounds(D, L, lane));
         }
         L.bptr[lane] = bp;
         L.blen[lane] = blen;
-        L.bsrc[lane] = bsrc;
+        L.bsrc[lane] = (int32_t)bq;
         uint32_t incl = blen;
 #pragma unroll
         for (uint32_t o = 1; o < 32; o <<= 1) {
@@ -720,17 +811,16 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
         // 2. flattened scan: element j belongs to the candidate l with pref[l-1] <= j < pref[l]
         uint32_t l = 0;
         const uint32_t nu = (P.tail_mode == SGE_TAIL_IEP) ? (T - 1 - t) : 0u;
+        const uint32_t ns = D.nsrc;
         for (uint32_t j = lane; j < total; j += 32) {
             while (L.pref[l] <= j) ++l;
             const uint32_t start = l ? L.pref[l - 1] : 0u;
             const uint32_t y = L.bptr[l][j - start];
-            const int bs = L.bsrc[l];
+            const uint32_t own = (uint32_t)L.bsrc[l];
             bool ok = true;
-            for_tail_lists(P, W, L, c, lc, l, i, [&](const uint32_t *p, uint32_t len, int src, bool pinned) {
-                if (src != bs) ok = in_list(W, c, p, len, src, pinned, y);
-                return ok;
-            });
-            if (ok) ok = !cand_excluded(P, W, L, lc, l, i, y);
+            for (uint32_t q = 0; q < ns && ok; ++q)
+                if (q != own) ok = td_has(D, L, W, c, q, l, y);
+            if (ok) ok = !td_excluded(D, L, l, y);
             if (!ok) continue;
             if (P.tail_mode == SGE_TAIL_SINGLE) {
                 ++single;
@@ -738,11 +828,14 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
                 atomicAdd(&L.cnt[l][1], 1u);
             } else {
                 uint32_t fm = 0;
-                for (uint32_t q = 0; q < nu; ++q) fm |= (uint32_t)in_tail_set(P, W, L, c, lc, l, i + 1 + q, y) << q;
-                // every subset s of fm: S[{t} ∪ (s shifted past t)] += 1
+                for (uint32_t q = t + 1; q < t + 1 + nu; ++q) {
+                    const uint32_t up = (ord >> (4 * q)) & 15u;
+                    fm |= (uint32_t)td_member(L.td[up], L, W, c, l, y) << up;
+                }
+                // every subset s of the later positions y belongs to: S[{tp} ∪ s] += 1
                 uint32_t s = fm;
                 while (true) {
-                    atomicAdd(&L.cnt[l][(1u << t) | (s << (t + 1))], 1u);
+                    atomicAdd(&L.cnt[l][(1u << tp) | s], 1u);
                     if (s == 0) break;
                     s = (s - 1) & fm;
                 }
@@ -790,6 +883,213 @@ __device__ unsigned long long leaf_roots(const DevPlan &P, WarpState &W, Ctx<STA
     return leaf_chunk(P, W, c, 0, n);
 }
 
+// Pair step helpers.  The leaf takes up to 32 queued (x, y) pairs as its
+// candidates with L0 = a: cm[l][0] = x (level a), cm[l][1] = y (level a+1).
+template <bool STATS>
+__device__ __forceinline__ unsigned long long pair_flush(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32_t a,
+                                                         uint32_t nq) {
+    LeafState &L = *c.L;
+    PairState &S = *c.PS;
+    const uint32_t lane = lane_id();
+    if (lane < nq) {
+        const uint32_t x = S.qx[lane], y = S.qy[lane];
+        L.cm[lane][0] = x;
+        L.cm[lane][1] = y;
+        if ((P.tail_par >> a) & 1u) nbr(c.g, x, L.cptr[lane][0], L.clen[lane][0]);
+        if ((P.tail_par >> (a + 1)) & 1u) nbr(c.g, y, L.cptr[lane][1], L.clen[lane][1]);
+    }
+    __syncwarp();
+    return leaf_chunk(P, W, c, a, nq);
+}
+
+// Level a+1's lists that are the same for every candidate x of level a
+// (matched levels below a only), its exclusion values, and whether N(x) is
+// one of its lists.  Mirrors build_level_wcoj / explore_level for level a+1.
+template <bool STATS>
+__device__ __forceinline__ void pair_sources(const DevPlan &P, const WarpState &W, const Ctx<STATS> &c,
+                                             uint32_t a) {
+    PairState &S = *c.PS;
+    const uint32_t i = a + 1;
+    if (lane_id() == 0) {
+        uint32_t ns = 0, xpar = (P.parents[i] >> a) & 1u;
+        if (P.join_style == SGE_JOIN_EXPLORATION) {
+            const uint32_t shared = P.parents[i] & ((1u << a) - 1u);
+            if (shared) {
+                const uint32_t lastp = 31 - __clz(shared);
+                if (P.slot[lastp][i] < 0 && lastp < 2 && W.pmode[lastp]) {
+                    S.sptr[ns] = W.lptr[lastp]; S.slen[ns] = W.llen[lastp]; S.stab[ns] = (int32_t)lastp;
+                } else {
+                    S.sptr[ns] = version_ptr(P, W, c, lastp, i); S.slen[ns] = W.vlen[lastp][i]; S.stab[ns] = -1;
+                }
+                ++ns;
+            }
+        } else {
+            uint32_t rem = P.parents[i];
+            if (P.base[i] >= 0) {
+                const uint32_t bl = (uint32_t)P.base[i];
+                S.sptr[ns] = W.flist[bl];
+                S.slen[ns] = W.fcnt[bl];
+                S.stab[ns] = (bl == 2 && ((P.pin_mask >> 2) & 1u) && W.pmode[2]) ? 2 : -1;
+                ++ns;
+                rem = P.rest[i];
+            }
+            for (uint32_t msk = rem & ((1u << a) - 1u); msk; msk &= msk - 1) {
+                const uint32_t j = __ffs(msk) - 1;
+                S.sptr[ns] = W.lptr[j];
+                S.slen[ns] = W.llen[j];
+                S.stab[ns] = (j < 2 && W.pmode[j]) ? (int32_t)j : -1;
+                ++ns;
+            }
+            xpar = (rem >> a) & 1u;
+        }
+        uint32_t nex = 0;
+        for (uint32_t msk = P.check[i] & ((1u << a) - 1u); msk; msk &= msk - 1) S.exv[nex++] = W.m[__ffs(msk) - 1];
+        S.ns = ns;
+        S.xpar = xpar;
+        S.nex = nex;
+    }
+    __syncwarp();
+}
+
+// y ∈ list q of level a+1 (shared list q, or N(x) for q = -1).
+template <bool STATS>
+__device__ __forceinline__ bool pair_in(const WarpState &W, const Ctx<STATS> &c, const PairState &S, int q,
+                                        uint32_t l, uint32_t y) {
+    if (q < 0) return contains(S.xp[l], S.xl[l], y);
+    if (S.stab[q] >= 0) return pin_has(c.tab + S.stab[q] * c.tw, W.pmode[S.stab[q]], c.tw, y);
+    return contains(S.sptr[q], S.slen[q], y);
+}
+
+// The last two enumerated levels as one step: for 32 candidates x of level
+// a = ne-2 at a time, level a+1's candidate sets are generated by one scan
+// flattened over (x, element) like the leaf's, and every surviving (x, y)
+// joins a queue the leaf drains 32 pairs at a time.  Same pairs as entering
+// level a+1 once per x (build_level_wcoj / explore_update + explore_level),
+// without one warp-wide set operation and one short leaf call per x.
+// Returns false on timeout.
+template <bool STATS>
+__device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32_t a, unsigned long long &acc) {
+    PairState &S = *c.PS;
+    const uint32_t lane = lane_id();
+    const uint32_t i = a + 1;
+    const uint32_t n = W.cnt[a];
+    const uint32_t *lst = W.list[a];
+    pair_sources(P, W, c, a);
+    const uint32_t ns = S.ns, xpar = S.xpar, nex = S.nex;
+    const bool ex_x = (P.check[i] >> a) & 1u;
+    uint32_t qn = 0;
+    bool ok = true;
+    for (uint32_t b0 = W.pos[a]; b0 < n; b0 += 32) {
+        if (out_of_time(c)) { ok = false; break; }
+        // 1. this batch's level-a candidates, compacted
+        const uint32_t idx = b0 + lane;
+        bool valid = idx < n;
+        const uint32_t xv = valid ? lst[idx] : 0u;
+        if (valid) valid = !excluded(P, W, a, xv);
+        const uint32_t bal = __ballot_sync(FULL_MASK, valid);
+        const uint32_t nc = __popc(bal);
+        if (valid) S.x[__popc(bal & ((1u << lane) - 1u))] = xv;
+        __syncwarp();
+        if (STATS) { c.partial += nc; c.set_ops += nc; }
+        // 2. per candidate: N(x), the list to scan (cheapest scan × probes), trimmed by level a+1's bounds
+        const uint32_t *bp = nullptr;
+        uint32_t blen = 0;
+        int32_t bsrc = -1;
+        if (lane < nc) {
+            const uint32_t x = S.x[lane];
+            const uint32_t *xp;
+            uint32_t xl;
+            nbr(c.g, x, xp, xl);
+            S.xp[lane] = xp;
+            S.xl[lane] = xl;
+            unsigned long long allp = 0, bestcost = ~0ull;
+            for (uint32_t q = 0; q < ns; ++q) allp += S.stab[q] >= 0 ? 1u : 2u + (31u - __clz(S.slen[q] + 1u));
+            const unsigned long long xcost = 2u + (31u - __clz(xl + 1u));
+            if (xpar) allp += xcost;
+            for (uint32_t q = 0; q < ns; ++q) {
+                const unsigned long long own = S.stab[q] >= 0 ? 1u : 2u + (31u - __clz(S.slen[q] + 1u));
+                const unsigned long long cost = (unsigned long long)S.slen[q] * (allp - own + 1);
+                if (cost < bestcost) { bestcost = cost; bp = S.sptr[q]; blen = S.slen[q]; bsrc = (int32_t)q; }
+            }
+            if (xpar) {
+                const unsigned long long cost = (unsigned long long)xl * (allp - xcost + 1);
+                if (cost < bestcost) { bestcost = cost; bp = xp; blen = xl; bsrc = -1; }
+            }
+            if (STATS) {
+                unsigned long long by = 4ull * blen;
+                for (uint32_t q = 0; q < ns; ++q)
+                    if ((int32_t)q != bsrc) by += 8ull + 4ull * S.slen[q];
+                if (xpar && bsrc != -1) by += 8ull + 4ull * xl;
+                c.alg_bytes += by;
+            }
+            Bounds b;
+            b.lo = 0;
+            b.hi = 0xFFFFFFFFu;
+            b.has_lo = P.lower[i] != 0;
+            b.has_hi = P.upper[i] != 0;
+            for (uint32_t msk = P.lower[i]; msk; msk &= msk - 1) {
+                const uint32_t p = __ffs(msk) - 1;
+                b.lo = max(b.lo, p == a ? x : W.m[p]);
+            }
+            for (uint32_t msk = P.upper[i]; msk; msk &= msk - 1) {
+                const uint32_t p = __ffs(msk) - 1;
+                b.hi = min(b.hi, p == a ? x : W.m[p]);
+            }
+            trim(bp, blen, b);
+        }
+        S.bp[lane] = bp;
+        S.bl[lane] = blen;
+        S.bs[lane] = bsrc;
+        uint32_t incl = blen;
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(FULL_MASK, incl, o);
+            if (lane >= o) incl += v;
+        }
+        S.pref[lane] = incl;
+        const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
+        __syncwarp();
+        // 3. flattened scan; survivors are appended to the pair queue
+        uint32_t l = 0;
+        for (uint32_t j0 = 0; j0 < total; j0 += 32) {
+            const uint32_t j = j0 + lane;
+            bool keep = j < total;
+            uint32_t y = 0;
+            if (keep) {
+                while (S.pref[l] <= j) ++l;
+                const uint32_t start = l ? S.pref[l - 1] : 0u;
+                y = S.bp[l][j - start];
+                const int32_t bs = S.bs[l];
+                for (uint32_t q = 0; q < ns && keep; ++q)
+                    if ((int32_t)q != bs) keep = pair_in(W, c, S, (int)q, l, y);
+                if (keep && xpar && bs != -1) keep = pair_in(W, c, S, -1, l, y);
+                for (uint32_t e = 0; e < nex && keep; ++e) keep = y != S.exv[e];
+                if (keep && ex_x) keep = y != S.x[l];
+            }
+            const uint32_t kb = __ballot_sync(FULL_MASK, keep);
+            if (keep) {
+                const uint32_t p = qn + __popc(kb & ((1u << lane) - 1u));
+                S.qx[p] = S.x[l];
+                S.qy[p] = y;
+            }
+            qn += __popc(kb);
+            if (STATS) c.partial += __popc(kb);
+            __syncwarp();
+            if (qn >= 32) {
+                acc += pair_flush(P, W, c, a, 32u);
+                // move the remainder (< 32 pairs) to the front of the queue
+                const uint32_t rx = S.qx[32 + lane], ry = S.qy[32 + lane];
+                __syncwarp();
+                if (lane < qn - 32) { S.qx[lane] = rx; S.qy[lane] = ry; }
+                qn -= 32;
+                __syncwarp();
+            }
+        }
+    }
+    if (ok && qn) acc += pair_flush(P, W, c, a, qn);
+    return ok;
+}
+
 // One root edge: DFS over levels 2..ne-2; the candidates of level ne-1 go to
 // the leaf 32 at a time.
 // Past the time budget?  (all lanes agree: lane 0 reads the clock)
@@ -814,6 +1114,7 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
     if (ne == 2) return leaf_roots(P, W, c, 1u, u, v);
     const bool explore = P.join_style == SGE_JOIN_EXPLORATION;
     const uint32_t L0 = ne - 1;
+    const uint32_t Lt = P.pair ? ne - 2 : L0;  // level whose candidates end the DFS
     LeafState &L = *c.L;
     set_match(c.g, W, 0, u);
     set_match(c.g, W, 1, v);
@@ -838,6 +1139,12 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
         __syncwarp();
     }
     while (ok) {
+        if (lv == Lt && P.pair) {
+            ok = pair_level(P, W, c, lv, acc);
+            if (lv == 2) break;
+            --lv;
+            continue;
+        }
         if (lv == L0) {
             const uint32_t n = W.cnt[lv];
             const uint32_t *lst = W.list[lv];
@@ -852,7 +1159,7 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
                 if (valid) {
                     const uint32_t rk = __popc(bal & ((1u << lane) - 1u));
                     L.cm[rk][0] = x;
-                    nbr(c.g, x, L.cptr[rk][0], L.clen[rk][0]);
+                    if ((P.tail_par >> L0) & 1u) nbr(c.g, x, L.cptr[rk][0], L.clen[rk][0]);
                 }
                 __syncwarp();
                 if (nc) acc += leaf_chunk(P, W, c, L0, nc);
@@ -889,11 +1196,11 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
     return ok ? acc : 0ull;
 }
 
-// Per-warp shared-memory carve-up: DevPlan | WarpState | LeafState | 3 tables.
+// Per-warp shared-memory carve-up: DevPlan | WarpState | LeafState | PairState | 3 tables.
 __host__ __device__ constexpr size_t align128(size_t x) { return (x + 127) & ~(size_t)127; }
 __host__ __device__ inline size_t warp_smem_bytes(uint32_t tw) {
     return align128(sizeof(DevPlan)) + align128(sizeof(WarpState)) + align128(sizeof(LeafState)) +
-           align128(3ull * tw * sizeof(uint32_t));
+           align128(sizeof(PairState)) + align128(3ull * tw * sizeof(uint32_t));
 }
 __device__ __forceinline__ DevPlan &warp_plan(unsigned char *smem, uint32_t wib, uint32_t tw) {
     return *reinterpret_cast<DevPlan *>(smem + (size_t)wib * warp_smem_bytes(tw));
@@ -905,7 +1212,9 @@ __device__ __forceinline__ WarpState &setup_warp(unsigned char *smem, uint32_t w
     unsigned char *base = smem + (size_t)wib * warp_smem_bytes(tw) + align128(sizeof(DevPlan));
     WarpState &W = *reinterpret_cast<WarpState *>(base);
     c.L = reinterpret_cast<LeafState *>(base + align128(sizeof(WarpState)));
-    c.tab = reinterpret_cast<uint32_t *>(base + align128(sizeof(WarpState)) + align128(sizeof(LeafState)));
+    c.PS = reinterpret_cast<PairState *>(base + align128(sizeof(WarpState)) + align128(sizeof(LeafState)));
+    c.tab = reinterpret_cast<uint32_t *>(base + align128(sizeof(WarpState)) + align128(sizeof(LeafState)) +
+                                         align128(sizeof(PairState)));
     c.tw = tw;
     c.tmode = tmode;
     const uint32_t fill = tmode == 2 ? PIN_EMPTY : 0u;
@@ -1237,6 +1546,25 @@ void to_devplan(const sge_plan_blob &b, DevPlan &d) {
                 d.hoist_at[i] = (uint8_t)(last < 1 ? 1u : last);
             }
         }
+    d.tail_par = 0;
+    for (uint32_t i = b.num_enum; i < b.k; ++i) d.tail_par |= b.parents[i];
+    // the pair step needs every tail list to be independent of level ne-2's
+    // per-candidate state: no tail reuses level ne-1's stored list, none is
+    // hoisted right after level ne-2, and (exploration) no tail's running
+    // list intersects N(m[ne-2]) into earlier parents, which the DFS would
+    // compute once per candidate of level ne-2 and the pair leaf per pair
+    d.pair = 0;
+    if (b.num_enum >= 4) {
+        const uint32_t a = b.num_enum - 2;
+        bool ok = true;
+        for (uint32_t i = b.num_enum; i < b.k; ++i) {
+            if (b.join_style == SGE_JOIN_WCOJ && b.base[i] == (int)(b.num_enum - 1)) ok = false;
+            if (((d.hoist_mask >> i) & 1u) && d.hoist_at[i] == a) ok = false;
+            if (b.join_style == SGE_JOIN_EXPLORATION && ((b.parents[i] >> a) & 1u) && (b.parents[i] & ((1u << a) - 1u)))
+                ok = false;
+        }
+        d.pair = ok ? 1u : 0u;
+    }
     d.mult = b.count_multiplier;
     d.chunk = 1;
     d.split_par = b.num_enum >= 3 ? (b.parents[2] & 3u) : 0u;
@@ -1397,12 +1725,20 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
     if (blocks * per_block > budget) blocks = std::max<size_t>(1, budget / std::max<size_t>(per_block, 1));
     L.blocks = blocks;
     L.scratch_bytes = blocks * per_block;
-    // heavy-root splitting (plans with >= 3 enumerated levels): roots whose
-    // level-2 list may exceed 4·S candidates run as tasks of S candidates
-    const uint32_t split_S = 128, split_H = 4 * split_S;
+    // heavy-root splitting (plans with >= 3 enumerated levels): a root whose
+    // level-2 list may exceed split_H candidates runs as tasks of S
+    // candidates.  A root's work grows with its level-2 list, and a warp's
+    // share of the launch is about ntasks × (mean endpoint degree M2/M1) /
+    // warps candidates; roots are split only when one could exceed a quarter
+    // of that share (splitting repeats the root's setup in every task)
+    const uint32_t split_S = 128;
     unsigned long long max_tasks = 1;
     const unsigned long long warps = blocks * L.wpb;
+    const double mean_deg = g->stats.moments[1] > 0 ? g->stats.moments[2] / g->stats.moments[1] : 1.0;
     for (auto &d : L.dps) {
+        const double share = (double)d.ntasks * mean_deg / (double)std::max<unsigned long long>(warps, 1);
+        const uint32_t split_H = o.heavy_threshold ? std::max(o.heavy_threshold, split_S)
+                                                   : (uint32_t)std::min(1e9, std::max(4.0 * split_S, share / 4.0));
         if (d.ne >= 3 && g->max_deg > split_H) {
             d.split_S = split_S;
             d.split_H = split_H;

@@ -79,7 +79,8 @@ class PlanOpts(C.Structure):
 
 class CountOpts(C.Structure):
     _fields_ = [("blocks_per_sm", u32), ("warps_per_block", u32), ("chunk", u32), ("time_budget_s", C.c_double),
-                ("max_level_capacity", u32), ("root_stride", u64), ("root_offset", u64), ("collect_counters", u32)]
+                ("max_level_capacity", u32), ("root_stride", u64), ("root_offset", u64), ("collect_counters", u32),
+                ("heavy_threshold", u32)]
 
 
 class Stats(C.Structure):
@@ -464,13 +465,15 @@ class Engine:
 
     def count(self, plans: list[PlanBlob], stats: bool = False, time_budget_s: float = 0.0,
               max_level_capacity: int = 0, blocks_per_sm: int = 0, warps_per_block: int = 0, chunk: int = 0,
-              root_stride: int = 1, root_offset: int = 0):
+              root_stride: int = 1, root_offset: int = 0, heavy_threshold: int = 0):
         """Counts every plan over the graph in one launch.  Returns (counts,
         instances, stats-dict); counts are the reference's "Number of matches"
         (uint64).  stats=True runs the instrumented kernel (set operations,
         algorithmic bytes); kernel_ms is reported either way.
         root_stride/root_offset restrict the run to root tasks
-        t ≡ root_offset (mod root_stride) (sharding, sampling)."""
+        t ≡ root_offset (mod root_stride) (sharding, sampling).  heavy_threshold
+        (0 = auto) splits roots whose level-2 list may exceed it into tasks of
+        a second launch."""
         handles = []
         try:
             for b in plans:
@@ -482,7 +485,7 @@ class Engine:
             inst = (u64 * len(plans))()
             st = Stats()
             o = CountOpts(blocks_per_sm, warps_per_block, chunk, time_budget_s, max_level_capacity, root_stride,
-                          root_offset, int(stats))
+                          root_offset, int(stats), heavy_threshold)
             _check(lib().sge_count(self._h, arr, len(plans), C.byref(o), counts, inst, C.byref(st)))
             return list(counts), list(inst), st.as_dict()
         finally:
@@ -536,7 +539,7 @@ class Batch:
 
     def __init__(self, engine: Engine, plans: list[PlanBlob], stats: bool = False, time_budget_s: float = 0.0,
                  blocks_per_sm: int = 0, warps_per_block: int = 0, chunk: int = 0, root_stride: int = 1,
-                 root_offset: int = 0):
+                 root_offset: int = 0, heavy_threshold: int = 0):
         self.engine = engine
         self.n = len(plans)
         self._ph = []
@@ -545,7 +548,8 @@ class Batch:
             _check(lib().sge_plan_create(C.byref(b), C.byref(ph)))
             self._ph.append(ph)
         arr = (C.c_void_p * self.n)(*[h.value for h in self._ph])
-        o = CountOpts(blocks_per_sm, warps_per_block, chunk, time_budget_s, 0, root_stride, root_offset, int(stats))
+        o = CountOpts(blocks_per_sm, warps_per_block, chunk, time_budget_s, 0, root_stride, root_offset, int(stats),
+                      heavy_threshold)
         h = C.c_void_p()
         try:
             _check(lib().sge_batch_create(engine._h, arr, self.n, C.byref(o), C.byref(h)))
