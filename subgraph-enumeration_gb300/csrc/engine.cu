@@ -74,6 +74,8 @@ struct DevPlan {
     uint32_t split_S;                             // level-2 candidates per deferred task (0 = never defer)
     uint32_t split_C;                             // deferred tasks per heavy root (max degree / S, rounded up)
     uint32_t pair;                                // 1: the last two enumerated levels run as one flattened step
+    uint32_t pair_direct;                         // pair step may count a single-list tail per pair inline
+    uint32_t epin;                                // exploration: tail level whose root-level running list is pinned
     uint32_t tail_par;                            // union of the tail levels' parents
 };
 static_assert(sizeof(DevPlan) % 4 == 0, "DevPlan is copied as 32-bit words");
@@ -147,6 +149,8 @@ struct PairState {
     int32_t bs[32];                   // scanned list: index into sptr, or -1 for N(x)
     uint32_t pref[32];
     uint32_t qx[64], qy[64];          // (x, y) pairs waiting for the leaf
+    uint32_t tr[32], tlo[32], thi[32];  // inline tail: count for x before y's own exclusion, x's range
+    TailDesc ptd;                     // inline tail: the tail level as seen from level a
 };
 
 constexpr uint32_t PIN_EMPTY = 0xFFFFFFFFu;
@@ -325,12 +329,23 @@ __device__ void pin_root(const DevPlan &P, WarpState &W, Ctx<STATS> &c) {
         if ((P.pin_mask >> j) & 1u) pin_list(W, c, j, W.lptr[j], W.llen[j]);
 }
 
+// Exploration: version (j, i) list pointer.
+template <bool STATS>
+__device__ __forceinline__ const uint32_t *version_ptr(const DevPlan &P, const WarpState &W, const Ctx<STATS> &c,
+                                                       uint32_t j, uint32_t i) {
+    int s = P.slot[j][i];
+    if (s < 0) return W.lptr[j];
+    return c.buf + (size_t)s * c.cap;
+}
+
 template <bool STATS>
 __device__ void unpin_root(const DevPlan &P, WarpState &W, Ctx<STATS> &c) {
     for (uint32_t j = 0; j < 2; ++j)
         if (W.pmode[j]) unpin_list(W, c, j, W.lptr[j], W.llen[j]);
     if (W.pmode[2]) {
-        if (W.hpin) unpin_list(W, c, 2, c.buf + (size_t)W.hpin * c.cap, W.hcnt[W.hpin]);
+        if (W.hpin && P.join_style == SGE_JOIN_EXPLORATION)
+            unpin_list(W, c, 2, version_ptr(P, W, c, 1, W.hpin), W.vlen[1][W.hpin]);
+        else if (W.hpin) unpin_list(W, c, 2, c.buf + (size_t)W.hpin * c.cap, W.hcnt[W.hpin]);
         else unpin_list(W, c, 2, W.flist[2], W.fcnt[2]);
     }
     __syncwarp();
@@ -491,14 +506,6 @@ __device__ __forceinline__ bool hoist_after(const DevPlan &P, WarpState &W, Ctx<
     return true;
 }
 
-// Exploration: version (j, i) list pointer.
-template <bool STATS>
-__device__ __forceinline__ const uint32_t *version_ptr(const DevPlan &P, const WarpState &W, const Ctx<STATS> &c,
-                                                       uint32_t j, uint32_t i) {
-    int s = P.slot[j][i];
-    if (s < 0) return W.lptr[j];
-    return c.buf + (size_t)s * c.cap;
-}
 
 // Exploration: after level j is matched, intersect N(m[j]) into the running
 // list of every later level that has j as a parent.  false = prune (empty) or
@@ -598,6 +605,8 @@ __device__ __forceinline__ void for_tail_lists(const DevPlan &P, const WarpState
         const uint32_t lastp = 31 - __clz(shared);
         if (P.slot[lastp][i] < 0 && lastp < 2 && W.pmode[lastp]) {
             if (!f(W.lptr[lastp], W.llen[lastp], (int)lastp, true)) return;
+        } else if (lastp == 1 && W.hpin == i) {
+            if (!f(version_ptr(P, W, c, 1, i), W.vlen[1][i], SRC_HOISTED, true)) return;
         } else if (!f(version_ptr(P, W, c, lastp, i), W.vlen[lastp][i], -1, false)) {
             return;
         }
@@ -960,6 +969,17 @@ __device__ __forceinline__ bool pair_in(const WarpState &W, const Ctx<STATS> &c,
     return contains(S.sptr[q], S.slen[q], y);
 }
 
+// v ∈ the inline tail's single list for batch candidate l.
+template <bool STATS>
+__device__ __forceinline__ bool pair_tail_has(const WarpState &W, const Ctx<STATS> &c, const PairState &S,
+                                              uint32_t l, uint32_t v) {
+    const TailDesc &D = S.ptd;
+    const uint32_t k = D.kind[0];
+    if (k < 3) return pin_has(c.tab + k * c.tw, W.pmode[k], c.tw, v);
+    if (k == 3) return contains(D.ptr[0], D.len[0], v);
+    return contains(S.xp[l], S.xl[l], v);
+}
+
 // The last two enumerated levels as one step: for 32 candidates x of level
 // a = ne-2 at a time, level a+1's candidate sets are generated by one scan
 // flattened over (x, element) like the leaf's, and every surviving (x, y)
@@ -975,9 +995,22 @@ __device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32
     const uint32_t n = W.cnt[a];
     const uint32_t *lst = W.list[a];
     pair_sources(P, W, c, a);
+    // inline tail: the tail level's single list does not depend on y, so the
+    // pair's count is x's count minus y itself when y is in x's range and list
+    bool inl = false;
+    if (P.pair_direct) {
+        if (lane == 0) {
+            const LeafCtx lc{a, P.join_style == SGE_JOIN_EXPLORATION};
+            tail_desc(P, W, *c.L, c, lc, P.ne, S.ptd);
+        }
+        __syncwarp();
+        inl = S.ptd.nsrc == 1;
+    }
+    const TailDesc &D = S.ptd;
     const uint32_t ns = S.ns, xpar = S.xpar, nex = S.nex;
     const bool ex_x = (P.check[i] >> a) & 1u;
     uint32_t qn = 0;
+    unsigned long long isum = 0;
     bool ok = true;
     for (uint32_t b0 = W.pos[a]; b0 < n; b0 += 32) {
         if (out_of_time(c)) { ok = false; break; }
@@ -1036,6 +1069,31 @@ __device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32
                 b.hi = min(b.hi, p == a ? x : W.m[p]);
             }
             trim(bp, blen, b);
+            if (inl) {
+                // x's tail count (range of the single list minus the matched values inside)
+                const uint32_t *fp = D.kind[0] == 4 ? xp : D.ptr[0];
+                const uint32_t fl = D.kind[0] == 4 ? xl : D.len[0];
+                Bounds tb;
+                tb.lo = D.lo;
+                tb.hi = D.hi;
+                tb.has_lo = D.has_lo;
+                tb.has_hi = D.has_hi;
+                if (D.lo_slots & 1u) tb.lo = max(tb.lo, x);
+                if (D.hi_slots & 1u) tb.hi = min(tb.hi, x);
+                const uint32_t *tp = fp;
+                uint32_t tl = fl;
+                trim(tp, tl, tb);
+                uint32_t cnt = tl;
+                for (uint32_t e = 0; e < D.nex + ((D.ex_slots & 1u) ? 1u : 0u); ++e) {
+                    const uint32_t v = e < D.nex ? D.exv[e] : x;
+                    if ((!tb.has_lo || v > tb.lo) && (!tb.has_hi || v < tb.hi) && pair_tail_has(W, c, S, lane, v))
+                        --cnt;
+                }
+                S.tr[lane] = cnt;
+                S.tlo[lane] = tb.has_lo ? tb.lo : 0u;
+                S.thi[lane] = tb.has_hi ? tb.hi : 0xFFFFFFFFu;
+                if (STATS) c.alg_bytes += 4ull * (2u + D.nex) * (31u - __clz(fl + 1u));
+            }
         }
         S.bp[lane] = bp;
         S.bl[lane] = blen;
@@ -1066,6 +1124,22 @@ __device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32
                 for (uint32_t e = 0; e < nex && keep; ++e) keep = y != S.exv[e];
                 if (keep && ex_x) keep = y != S.x[l];
             }
+            if (inl) {
+                if (keep) {
+                    uint32_t r = S.tr[l];
+                    // y itself, when the tail excludes it and it lies in x's range and list
+                    if ((D.ex_slots & 2u) && (!D.has_lo || y > S.tlo[l]) && (!D.has_hi || y < S.thi[l]) &&
+                        pair_tail_has(W, c, S, l, y))
+                        --r;
+                    isum += r;
+                }
+                if (STATS) {
+                    const uint32_t kb = __ballot_sync(FULL_MASK, keep);
+                    c.partial += __popc(kb);
+                    c.set_ops += __popc(kb);
+                }
+                continue;
+            }
             const uint32_t kb = __ballot_sync(FULL_MASK, keep);
             if (keep) {
                 const uint32_t p = qn + __popc(kb & ((1u << lane) - 1u));
@@ -1087,6 +1161,7 @@ __device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32
         }
     }
     if (ok && qn) acc += pair_flush(P, W, c, a, qn);
+    if (inl) acc += warp_sum_u64(isum);
     return ok;
 }
 
@@ -1121,8 +1196,17 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
     if (P.pin_mask) pin_root(P, W, c);
     unsigned long long acc = 0;
     bool ok = true;
-    if (explore) ok = explore_update(P, W, c, 0) && explore_update(P, W, c, 1);
-    else if (P.hoist_mask) ok = hoist_after(P, W, c, 1);
+    if (explore) {
+        ok = explore_update(P, W, c, 0) && explore_update(P, W, c, 1);
+        if (ok && P.epin && c.tmode && W.pmode[2] == 0u) {
+            pin_list(W, c, 2, version_ptr(P, W, c, 1, P.epin), W.vlen[1][P.epin]);
+            __syncwarp();
+            if (lane == 0 && W.pmode[2]) W.hpin = P.epin;
+            __syncwarp();
+        }
+    } else if (P.hoist_mask) {
+        ok = hoist_after(P, W, c, 1);
+    }
     uint32_t lv = 2;
     if (ok) {
         if (explore) explore_level(P, W, c, lv);
@@ -1564,6 +1648,22 @@ void to_devplan(const sge_plan_blob &b, DevPlan &d) {
                 ok = false;
         }
         d.pair = ok ? 1u : 0u;
+    }
+    // a single tail level that neither has level ne-1 as a parent nor is
+    // bounded by it is counted per pair without the leaf, when its lists
+    // reduce to one at run time (the count only drops y itself)
+    const uint32_t last = b.num_enum - 1;
+    d.pair_direct = (d.pair && b.tail_mode == SGE_TAIL_SINGLE && b.tail_len == 1 && b.num_enum < b.k &&
+                     !(((b.parents[b.num_enum] | b.lower[b.num_enum] | b.upper[b.num_enum]) >> last) & 1u))
+                        ? 1u : 0u;
+    // exploration: the running list of a tail level whose parents below the
+    // leaf are exactly levels 0 and 1 is final once the root is matched;
+    // it is pinned in the third table
+    d.epin = 0;
+    if (b.join_style == SGE_JOIN_EXPLORATION && b.num_enum >= 3) {
+        const uint32_t lt = d.pair ? b.num_enum - 2 : b.num_enum - 1;
+        for (uint32_t i = b.num_enum; i < b.k && !d.epin; ++i)
+            if ((b.parents[i] & ((1u << lt) - 1u)) == 3u) d.epin = i;
     }
     d.mult = b.count_multiplier;
     d.chunk = 1;
