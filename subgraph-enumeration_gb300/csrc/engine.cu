@@ -36,6 +36,8 @@ using namespace sge;
 
 #define FULL_MASK 0xFFFFFFFFu
 #define SGE_MAX_BUFS 32
+// exploration version slots: at most Σ_{i<16} (i-1) = 105 for k <= 16
+#define SGE_MAX_VSLOTS 112
 
 namespace {
 
@@ -97,7 +99,7 @@ struct WarpState {
     uint32_t fcnt[SGE_MAX_K];
     const uint32_t *lptr[SGE_MAX_K];      // N(m[j]) of the matched levels
     uint32_t llen[SGE_MAX_K];
-    uint32_t vlen[SGE_MAX_K][SGE_MAX_K];  // exploration version lengths (j, i)
+    uint32_t vslot[SGE_MAX_VSLOTS];       // exploration: length of the version list in each buffer slot
     uint32_t pmode[3];                    // pinned N(m[0]), N(m[1]), level-2 list: 0 none, 1 bitmap, 2 hash
     uint32_t hcnt[SGE_MAX_K];             // hoisted tail lists (buffer slot = level)
     uint32_t hpin;                        // tail level whose hoisted list is pinned in table 2 (0 = none)
@@ -119,15 +121,11 @@ struct TailDesc {
 // Leaf state (shared memory): up to 32 candidates of the last enumerated
 // level, each with its own matched values for the levels from L0 on.
 struct LeafState {
-    TailDesc td[SGE_MAX_TAIL];
     uint32_t cm[32][2];
     const uint32_t *cptr[32][2];
     uint32_t clen[32][2];
     const uint32_t *bptr[32];
-    uint32_t blen[32];
-    int32_t bsrc[32];
     uint32_t pref[32];
-    uint32_t cnt[32][16];
 };
 
 // Pair step (shared memory): level a = ne-2 of the DFS is processed 32
@@ -145,8 +143,6 @@ struct PairState {
     const uint32_t *xp[32];           // N(x)
     uint32_t xl[32];
     const uint32_t *bp[32];           // list scanned for candidate x (trimmed by bounds)
-    uint32_t bl[32];
-    int32_t bs[32];                   // scanned list: index into sptr, or -1 for N(x)
     uint32_t pref[32];
     uint32_t qx[64], qy[64];          // (x, y) pairs waiting for the leaf
     uint32_t tr[32], tlo[32], thi[32];  // inline tail: count for x before y's own exclusion, x's range
@@ -248,6 +244,9 @@ struct Ctx {
     uint32_t tmode;   // 0 none, 1 bitmap over all vertices, 2 open-addressing hash
     LeafState *L;
     PairState *PS;
+    TailDesc *td;     // this warp's tail descriptors (one per inclusion–exclusion pass)
+    uint32_t *cnt;    // per-candidate counters S[subset]: cnt[l * cs + subset]
+    uint32_t cs;
     unsigned long long tstart, deadline;  // globaltimer of the warp's start; budget in ns (0 = none)
     unsigned long long set_ops, alg_bytes, partial;
 };
@@ -329,7 +328,13 @@ __device__ void pin_root(const DevPlan &P, WarpState &W, Ctx<STATS> &c) {
         if ((P.pin_mask >> j) & 1u) pin_list(W, c, j, W.lptr[j], W.llen[j]);
 }
 
-// Exploration: version (j, i) list pointer.
+// Exploration: version (j, i) list length and pointer.  The first parent's
+// version is N(m[j]) itself; the others live in buffer slot[j][i].
+__device__ __forceinline__ uint32_t version_len(const DevPlan &P, const WarpState &W, uint32_t j, uint32_t i) {
+    const int s = P.slot[j][i];
+    return s < 0 ? W.llen[j] : W.vslot[s];
+}
+
 template <bool STATS>
 __device__ __forceinline__ const uint32_t *version_ptr(const DevPlan &P, const WarpState &W, const Ctx<STATS> &c,
                                                        uint32_t j, uint32_t i) {
@@ -344,7 +349,7 @@ __device__ void unpin_root(const DevPlan &P, WarpState &W, Ctx<STATS> &c) {
         if (W.pmode[j]) unpin_list(W, c, j, W.lptr[j], W.llen[j]);
     if (W.pmode[2]) {
         if (W.hpin && P.join_style == SGE_JOIN_EXPLORATION)
-            unpin_list(W, c, 2, version_ptr(P, W, c, 1, W.hpin), W.vlen[1][W.hpin]);
+            unpin_list(W, c, 2, version_ptr(P, W, c, 1, W.hpin), version_len(P, W, 1, W.hpin));
         else if (W.hpin) unpin_list(W, c, 2, c.buf + (size_t)W.hpin * c.cap, W.hcnt[W.hpin]);
         else unpin_list(W, c, 2, W.flist[2], W.fcnt[2]);
     }
@@ -518,14 +523,13 @@ __device__ __forceinline__ bool explore_update(const DevPlan &P, WarpState &W, C
         uint32_t below = P.parents[i] & ((1u << j) - 1u);
         if (below == 0) {
             __syncwarp();
-            if (lane == 0) W.vlen[j][i] = W.llen[j];
             __syncwarp();
             if (W.llen[j] == 0) return false;
             continue;
         }
         uint32_t pj = 31 - __clz(below);  // previous parent of i
         const uint32_t *prev = version_ptr(P, W, c, pj, i);
-        uint32_t plen = W.vlen[pj][i];
+        uint32_t plen = version_len(P, W, pj, i);
         uint32_t *out = c.buf + (size_t)P.slot[j][i] * c.cap;
         if (STATS) { c.set_ops += 1; c.alg_bytes += 8ull + 4ull * (plen + W.llen[j]); }
         uint32_t total = 0;
@@ -545,7 +549,7 @@ __device__ __forceinline__ bool explore_update(const DevPlan &P, WarpState &W, C
             total += __popc(bal);
         }
         __syncwarp();
-        if (lane == 0) W.vlen[j][i] = total;
+        if (lane == 0) W.vslot[P.slot[j][i]] = total;
         __syncwarp();
         if (total > c.cap) {
             if (lane == 0) atomicOr(c.flags, FLAG_OVERFLOW);
@@ -561,7 +565,7 @@ template <bool STATS>
 __device__ __forceinline__ void explore_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32_t i) {
     uint32_t lastp = 31 - __clz(P.parents[i]);
     const uint32_t *bp = version_ptr(P, W, c, lastp, i);
-    uint32_t blen = W.vlen[lastp][i];
+    uint32_t blen = version_len(P, W, lastp, i);
     Bounds b = level_bounds(P, W, i);
     __syncwarp();
     if (lane_id() == 0) { W.flist[i] = bp; W.fcnt[i] = blen; }
@@ -606,8 +610,8 @@ __device__ __forceinline__ void for_tail_lists(const DevPlan &P, const WarpState
         if (P.slot[lastp][i] < 0 && lastp < 2 && W.pmode[lastp]) {
             if (!f(W.lptr[lastp], W.llen[lastp], (int)lastp, true)) return;
         } else if (lastp == 1 && W.hpin == i) {
-            if (!f(version_ptr(P, W, c, 1, i), W.vlen[1][i], SRC_HOISTED, true)) return;
-        } else if (!f(version_ptr(P, W, c, lastp, i), W.vlen[lastp][i], -1, false)) {
+            if (!f(version_ptr(P, W, c, 1, i), version_len(P, W, 1, i), SRC_HOISTED, true)) return;
+        } else if (!f(version_ptr(P, W, c, lastp, i), version_len(P, W, lastp, i), -1, false)) {
             return;
         }
         shared = 0;
@@ -736,10 +740,9 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
     const uint32_t passes = (P.tail_mode == SGE_TAIL_IEP) ? T : 1u;
     // lane t describes tail level ne+t (IEP passes probe the later levels too)
     __syncwarp();
-    if (lane < passes) tail_desc(P, W, L, c, lc, ne + lane, L.td[lane]);
+    if (lane < passes) tail_desc(P, W, L, c, lc, ne + lane, c.td[lane]);
     if (P.tail_mode != SGE_TAIL_SINGLE) {
-#pragma unroll
-        for (uint32_t q = 0; q < 16; ++q) L.cnt[lane][q] = 0;
+        for (uint32_t q = 0; q < c.cs; ++q) c.cnt[lane * c.cs + q] = 0;
     }
     __syncwarp();
     // inclusion–exclusion: S[A] (A a set of tail positions) is counted in the
@@ -751,14 +754,14 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
     if (passes > 1) {
         uint32_t n = 0;
         for (uint32_t q = 0; q < passes; ++q)
-            if (L.td[q].nsrc != 1) ord |= q << (4 * n++);
+            if (c.td[q].nsrc != 1) ord |= q << (4 * n++);
         for (uint32_t q = 0; q < passes; ++q)
-            if (L.td[q].nsrc == 1) ord |= q << (4 * n++);
+            if (c.td[q].nsrc == 1) ord |= q << (4 * n++);
     }
     unsigned long long single = 0, bytes = 0;
     for (uint32_t t = 0; t < passes; ++t) {
         const uint32_t tp = (ord >> (4 * t)) & 15u;
-        const TailDesc &D = L.td[tp];
+        const TailDesc &D = c.td[tp];
         // a tail level with a single list (after reuse) is counted without a
         // scan: range size minus the matched vertices inside it (numResults)
         // (the last inclusion–exclusion pass probes no other tail level, so it
@@ -780,34 +783,42 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
                 if (D.ex_slots & 1u) drop(L.cm[lane][0]);
                 if (D.ex_slots & 2u) drop(L.cm[lane][1]);
                 if (P.tail_mode == SGE_TAIL_SINGLE) single += cnt;
-                else if (P.tail_mode == SGE_TAIL_CHOOSE) L.cnt[lane][1] = cnt;
-                else L.cnt[lane][1u << tp] = cnt;
+                else if (P.tail_mode == SGE_TAIL_CHOOSE) c.cnt[(lane) * c.cs + (1)] = cnt;
+                else c.cnt[(lane) * c.cs + (1u << tp)] = cnt;
                 if (STATS) bytes += 4ull * (2u + __popc(P.check[ne + tp])) * (31u - __clz(blen + 1u));
             }
             __syncwarp();
             continue;
         }
-        // 1. each candidate scans its cheapest list (scan length × probes of the others), trimmed by its bounds
-        const uint32_t *bp = nullptr;
-        uint32_t blen = 0, bq = 0;
-        if (lane < ncand) {
-            unsigned long long allp = 0, bestcost = ~0ull;
-            for (uint32_t q = 0; q < D.nsrc; ++q)
-                allp += D.kind[q] < 3 ? 1u : 2u + (31u - __clz(td_len(D, L, q, lane) + 1u));
+        // 1. the warp scans one source per candidate, the one with the least
+        // cost summed over the candidates (scan length × probes of the
+        // others), trimmed by each candidate's bounds; the others are probed
+        uint32_t bq = 0;
+        {
+            unsigned long long allp = 0, best = ~0ull;
+            if (lane < ncand)
+                for (uint32_t q = 0; q < D.nsrc; ++q)
+                    allp += D.kind[q] < 3 ? 1u : 2u + (31u - __clz(td_len(D, L, q, lane) + 1u));
             for (uint32_t q = 0; q < D.nsrc; ++q) {
-                const uint32_t len = td_len(D, L, q, lane);
-                const unsigned long long own = D.kind[q] < 3 ? 1u : 2u + (31u - __clz(len + 1u));
-                const unsigned long long cost = (unsigned long long)len * (allp - own + 1);
-                if (cost < bestcost) { bestcost = cost; bq = q; }
-                if (STATS) bytes += 4ull * len;
+                unsigned long long cost = 0;
+                if (lane < ncand) {
+                    const uint32_t len = td_len(D, L, q, lane);
+                    const unsigned long long own = D.kind[q] < 3 ? 1u : 2u + (31u - __clz(len + 1u));
+                    cost = (unsigned long long)len * (allp - own + 1);
+                    if (STATS) bytes += 4ull * len;
+                }
+                cost = warp_sum_u64(cost);
+                if (cost < best) { best = cost; bq = q; }
             }
+        }
+        const uint32_t *bp = nullptr;
+        uint32_t blen = 0;
+        if (lane < ncand) {
             bp = td_ptr(D, L, bq, lane);
             blen = td_len(D, L, bq, lane);
             trim(bp, blen, td_bounds(D, L, lane));
         }
         L.bptr[lane] = bp;
-        L.blen[lane] = blen;
-        L.bsrc[lane] = (int32_t)bq;
         uint32_t incl = blen;
 #pragma unroll
         for (uint32_t o = 1; o < 32; o <<= 1) {
@@ -817,34 +828,33 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
         L.pref[lane] = incl;
         const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
         __syncwarp();
+        const uint32_t ns = D.nsrc;
+        const uint32_t nu = (P.tail_mode == SGE_TAIL_IEP) ? (T - 1 - t) : 0u;
         // 2. flattened scan: element j belongs to the candidate l with pref[l-1] <= j < pref[l]
         uint32_t l = 0;
-        const uint32_t nu = (P.tail_mode == SGE_TAIL_IEP) ? (T - 1 - t) : 0u;
-        const uint32_t ns = D.nsrc;
         for (uint32_t j = lane; j < total; j += 32) {
             while (L.pref[l] <= j) ++l;
             const uint32_t start = l ? L.pref[l - 1] : 0u;
             const uint32_t y = L.bptr[l][j - start];
-            const uint32_t own = (uint32_t)L.bsrc[l];
             bool ok = true;
             for (uint32_t q = 0; q < ns && ok; ++q)
-                if (q != own) ok = td_has(D, L, W, c, q, l, y);
+                if (q != bq) ok = td_has(D, L, W, c, q, l, y);
             if (ok) ok = !td_excluded(D, L, l, y);
             if (!ok) continue;
             if (P.tail_mode == SGE_TAIL_SINGLE) {
                 ++single;
             } else if (P.tail_mode == SGE_TAIL_CHOOSE) {
-                atomicAdd(&L.cnt[l][1], 1u);
+                atomicAdd(&c.cnt[(l) * c.cs + (1)], 1u);
             } else {
                 uint32_t fm = 0;
                 for (uint32_t q = t + 1; q < t + 1 + nu; ++q) {
                     const uint32_t up = (ord >> (4 * q)) & 15u;
-                    fm |= (uint32_t)td_member(L.td[up], L, W, c, l, y) << up;
+                    fm |= (uint32_t)td_member(c.td[up], L, W, c, l, y) << up;
                 }
                 // every subset s of the later positions y belongs to: S[{tp} ∪ s] += 1
                 uint32_t s = fm;
                 while (true) {
-                    atomicAdd(&L.cnt[l][(1u << tp) | s], 1u);
+                    atomicAdd(&c.cnt[(l) * c.cs + ((1u << tp) | s)], 1u);
                     if (s == 0) break;
                     s = (s - 1) & fm;
                 }
@@ -858,11 +868,11 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
         r = single;
     } else if (lane < ncand) {
         if (P.tail_mode == SGE_TAIL_CHOOSE) {
-            r = binom_exact(L.cnt[lane][1], T);
+            r = binom_exact(c.cnt[(lane) * c.cs + (1)], T);
         } else {
             for (uint32_t p = 0; p < P.nparts; ++p) {
                 unsigned long long term = (unsigned long long)(long long)P.part_coef[p];
-                for (uint32_t bk = 0; bk < P.part_nblocks[p]; ++bk) term *= L.cnt[lane][P.part_block[p][bk]];
+                for (uint32_t bk = 0; bk < P.part_nblocks[p]; ++bk) term *= c.cnt[lane * c.cs + P.part_block[p][bk]];
                 r += term;
             }
         }
@@ -928,7 +938,7 @@ __device__ __forceinline__ void pair_sources(const DevPlan &P, const WarpState &
                 if (P.slot[lastp][i] < 0 && lastp < 2 && W.pmode[lastp]) {
                     S.sptr[ns] = W.lptr[lastp]; S.slen[ns] = W.llen[lastp]; S.stab[ns] = (int32_t)lastp;
                 } else {
-                    S.sptr[ns] = version_ptr(P, W, c, lastp, i); S.slen[ns] = W.vlen[lastp][i]; S.stab[ns] = -1;
+                    S.sptr[ns] = version_ptr(P, W, c, lastp, i); S.slen[ns] = version_len(P, W, lastp, i); S.stab[ns] = -1;
                 }
                 ++ns;
             }
@@ -1024,30 +1034,40 @@ __device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32
         if (valid) S.x[__popc(bal & ((1u << lane) - 1u))] = xv;
         __syncwarp();
         if (STATS) { c.partial += nc; c.set_ops += nc; }
-        // 2. per candidate: N(x), the list to scan (cheapest scan × probes), trimmed by level a+1's bounds
+        // 2. per candidate: N(x); the warp scans one source for every
+        // candidate (the least cost summed over the batch: scan length ×
+        // probes of the others), trimmed by level a+1's bounds
         const uint32_t *bp = nullptr;
         uint32_t blen = 0;
         int32_t bsrc = -1;
+        uint32_t x = 0, xl = 0;
+        const uint32_t *xp = nullptr;
         if (lane < nc) {
-            const uint32_t x = S.x[lane];
-            const uint32_t *xp;
-            uint32_t xl;
+            x = S.x[lane];
             nbr(c.g, x, xp, xl);
             S.xp[lane] = xp;
             S.xl[lane] = xl;
-            unsigned long long allp = 0, bestcost = ~0ull;
+        }
+        {
+            unsigned long long allp = 0;
             for (uint32_t q = 0; q < ns; ++q) allp += S.stab[q] >= 0 ? 1u : 2u + (31u - __clz(S.slen[q] + 1u));
             const unsigned long long xcost = 2u + (31u - __clz(xl + 1u));
             if (xpar) allp += xcost;
+            unsigned long long best = ~0ull;
             for (uint32_t q = 0; q < ns; ++q) {
                 const unsigned long long own = S.stab[q] >= 0 ? 1u : 2u + (31u - __clz(S.slen[q] + 1u));
-                const unsigned long long cost = (unsigned long long)S.slen[q] * (allp - own + 1);
-                if (cost < bestcost) { bestcost = cost; bp = S.sptr[q]; blen = S.slen[q]; bsrc = (int32_t)q; }
+                const unsigned long long cost =
+                    warp_sum_u64(lane < nc ? (unsigned long long)S.slen[q] * (allp - own + 1) : 0ull);
+                if (cost < best) { best = cost; bsrc = (int32_t)q; }
             }
             if (xpar) {
-                const unsigned long long cost = (unsigned long long)xl * (allp - xcost + 1);
-                if (cost < bestcost) { bestcost = cost; bp = xp; blen = xl; bsrc = -1; }
+                const unsigned long long cost = warp_sum_u64(lane < nc ? (unsigned long long)xl * (allp - xcost + 1) : 0ull);
+                if (cost < best) { best = cost; bsrc = -1; }
             }
+        }
+        if (lane < nc) {
+            bp = bsrc < 0 ? xp : S.sptr[bsrc];
+            blen = bsrc < 0 ? xl : S.slen[bsrc];
             if (STATS) {
                 unsigned long long by = 4ull * blen;
                 for (uint32_t q = 0; q < ns; ++q)
@@ -1096,8 +1116,6 @@ __device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32
             }
         }
         S.bp[lane] = bp;
-        S.bl[lane] = blen;
-        S.bs[lane] = bsrc;
         uint32_t incl = blen;
 #pragma unroll
         for (uint32_t o = 1; o < 32; o <<= 1) {
@@ -1117,10 +1135,9 @@ __device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32
                 while (S.pref[l] <= j) ++l;
                 const uint32_t start = l ? S.pref[l - 1] : 0u;
                 y = S.bp[l][j - start];
-                const int32_t bs = S.bs[l];
                 for (uint32_t q = 0; q < ns && keep; ++q)
-                    if ((int32_t)q != bs) keep = pair_in(W, c, S, (int)q, l, y);
-                if (keep && xpar && bs != -1) keep = pair_in(W, c, S, -1, l, y);
+                    if ((int32_t)q != bsrc) keep = pair_in(W, c, S, (int)q, l, y);
+                if (keep && xpar && bsrc != -1) keep = pair_in(W, c, S, -1, l, y);
                 for (uint32_t e = 0; e < nex && keep; ++e) keep = y != S.exv[e];
                 if (keep && ex_x) keep = y != S.x[l];
             }
@@ -1199,7 +1216,7 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
     if (explore) {
         ok = explore_update(P, W, c, 0) && explore_update(P, W, c, 1);
         if (ok && P.epin && c.tmode && W.pmode[2] == 0u) {
-            pin_list(W, c, 2, version_ptr(P, W, c, 1, P.epin), W.vlen[1][P.epin]);
+            pin_list(W, c, 2, version_ptr(P, W, c, 1, P.epin), version_len(P, W, 1, P.epin));
             __syncwarp();
             if (lane == 0 && W.pmode[2]) W.hpin = P.epin;
             __syncwarp();
@@ -1280,25 +1297,33 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
     return ok ? acc : 0ull;
 }
 
-// Per-warp shared-memory carve-up: DevPlan | WarpState | LeafState | PairState | 3 tables.
+// Per-warp shared-memory carve-up: WarpState | LeafState | PairState |
+// ntd tail descriptors | 32 × cs leaf counters | 3 pinned-list tables.  The
+// plans themselves stay in global memory (read through L1): the fewer bytes a
+// warp holds, the more warps are resident, and the DFS is latency-bound.
 __host__ __device__ constexpr size_t align128(size_t x) { return (x + 127) & ~(size_t)127; }
-__host__ __device__ inline size_t warp_smem_bytes(uint32_t tw) {
-    return align128(sizeof(DevPlan)) + align128(sizeof(WarpState)) + align128(sizeof(LeafState)) +
-           align128(sizeof(PairState)) + align128(3ull * tw * sizeof(uint32_t));
-}
-__device__ __forceinline__ DevPlan &warp_plan(unsigned char *smem, uint32_t wib, uint32_t tw) {
-    return *reinterpret_cast<DevPlan *>(smem + (size_t)wib * warp_smem_bytes(tw));
+__host__ __device__ inline size_t warp_smem_bytes(uint32_t tw, uint32_t ntd, uint32_t cs) {
+    return align128(sizeof(WarpState)) + align128(sizeof(LeafState)) + align128(sizeof(PairState)) +
+           align128(ntd * sizeof(TailDesc)) + align128(32ull * cs * sizeof(uint32_t)) +
+           align128(3ull * tw * sizeof(uint32_t));
 }
 
 template <bool STATS>
 __device__ __forceinline__ WarpState &setup_warp(unsigned char *smem, uint32_t wib, uint32_t tw, uint32_t tmode,
-                                                 Ctx<STATS> &c) {
-    unsigned char *base = smem + (size_t)wib * warp_smem_bytes(tw) + align128(sizeof(DevPlan));
+                                                 uint32_t ntd, uint32_t cs, Ctx<STATS> &c) {
+    unsigned char *base = smem + (size_t)wib * warp_smem_bytes(tw, ntd, cs);
     WarpState &W = *reinterpret_cast<WarpState *>(base);
-    c.L = reinterpret_cast<LeafState *>(base + align128(sizeof(WarpState)));
-    c.PS = reinterpret_cast<PairState *>(base + align128(sizeof(WarpState)) + align128(sizeof(LeafState)));
-    c.tab = reinterpret_cast<uint32_t *>(base + align128(sizeof(WarpState)) + align128(sizeof(LeafState)) +
-                                         align128(sizeof(PairState)));
+    base += align128(sizeof(WarpState));
+    c.L = reinterpret_cast<LeafState *>(base);
+    base += align128(sizeof(LeafState));
+    c.PS = reinterpret_cast<PairState *>(base);
+    base += align128(sizeof(PairState));
+    c.td = reinterpret_cast<TailDesc *>(base);
+    base += align128(ntd * sizeof(TailDesc));
+    c.cnt = reinterpret_cast<uint32_t *>(base);
+    c.cs = cs;
+    base += align128(32ull * cs * sizeof(uint32_t));
+    c.tab = reinterpret_cast<uint32_t *>(base);
     c.tw = tw;
     c.tmode = tmode;
     const uint32_t fill = tmode == 2 ? PIN_EMPTY : 0u;
@@ -1306,6 +1331,12 @@ __device__ __forceinline__ WarpState &setup_warp(unsigned char *smem, uint32_t w
     if (lane_id() == 0) { W.pmode[0] = 0; W.pmode[1] = 0; W.pmode[2] = 0; W.hpin = 0; }
     __syncwarp();
     return W;
+}
+
+// Tail descriptors and counters one plan's leaf needs.
+__host__ __device__ inline uint32_t plan_ntd(const DevPlan &d) { return d.tail_mode == SGE_TAIL_IEP ? d.T : 1u; }
+__host__ __device__ inline uint32_t plan_cs(const DevPlan &d) {
+    return d.tail_mode == SGE_TAIL_IEP ? (1u << d.T) : (d.tail_mode == SGE_TAIL_CHOOSE ? 2u : 1u);
 }
 
 // Root task t of plan P -> directed root edge (u, v).
@@ -1341,11 +1372,11 @@ __global__ void __launch_bounds__(256, 3) count_kernel(DevGraph g, const DevPlan
                                                     uint32_t *scratch, uint32_t cap, uint32_t bufs_per_warp,
                                                     uint32_t tw, uint32_t tmode, unsigned long long deadline_ns,
                                                     uint32_t *flags, DevStats *stats, uint32_t phase,
-                                                    uint32_t *heavy_cnt, uint32_t *heavy_ids, uint32_t heavy_cap) {
+                                                    uint32_t *heavy_cnt, uint32_t *heavy_ids, uint32_t heavy_cap,
+                                                    uint32_t ntd, uint32_t cs) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t lane = lane_id();
     const uint32_t wib = threadIdx.x >> 5;
-    DevPlan &P = warp_plan(smem_raw, wib, tw);
     const size_t gwarp = (size_t)blockIdx.x * (blockDim.x >> 5) + wib;
     Ctx<STATS> c;
     c.g = g;
@@ -1353,7 +1384,7 @@ __global__ void __launch_bounds__(256, 3) count_kernel(DevGraph g, const DevPlan
     c.cap = cap;
     c.flags = flags;
     c.set_ops = c.alg_bytes = c.partial = 0;
-    WarpState &W = setup_warp(smem_raw, wib, tw, tmode, c);
+    WarpState &W = setup_warp(smem_raw, wib, tw, tmode, ntd, cs, c);
     unsigned long long roots = 0;
     unsigned long long tstart = 0;
     if (lane == 0) tstart = globaltimer_ns();
@@ -1364,15 +1395,12 @@ __global__ void __launch_bounds__(256, 3) count_kernel(DevGraph g, const DevPlan
     uint32_t cur = 0;
     unsigned long long acc = 0, ntasks = 0;
     auto load_plan = [&](uint32_t pi) {
-        __syncwarp();
-        const uint32_t *src = reinterpret_cast<const uint32_t *>(plans + pi);
-        uint32_t *dst = reinterpret_cast<uint32_t *>(&P);
-        for (uint32_t w = lane; w < sizeof(DevPlan) / 4; w += 32) dst[w] = src[w];
-        __syncwarp();
-        ntasks = phase == 0 ? P.ntasks : (unsigned long long)min(heavy_cnt[pi], heavy_cap) * P.split_C;
+        const DevPlan &Q = plans[pi];
+        ntasks = phase == 0 ? Q.ntasks : (unsigned long long)min(heavy_cnt[pi], heavy_cap) * Q.split_C;
     };
     if (nplans) load_plan(0);
     while (cur < nplans) {
+        const DevPlan &P = plans[cur];
         if (out_of_time(c)) break;
         if (*(volatile uint32_t *)flags & FLAG_OVERFLOW) break;
         const uint32_t chunk = phase == 0 ? P.chunk : 1u;
@@ -1445,7 +1473,7 @@ __global__ void __launch_bounds__(256) enum_kernel(DevGraph g, const DevPlan *__
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t lane = lane_id();
     const uint32_t wib = threadIdx.x >> 5;
-    DevPlan &P = warp_plan(smem_raw, wib, 0u);
+    const DevPlan &P = *plan;
     const size_t gwarp = (size_t)blockIdx.x * (blockDim.x >> 5) + wib;
     Ctx<false> c;
     c.g = g;
@@ -1455,13 +1483,7 @@ __global__ void __launch_bounds__(256) enum_kernel(DevGraph g, const DevPlan *__
     c.set_ops = c.alg_bytes = c.partial = 0;
     c.tstart = 0;
     c.deadline = 0;
-    WarpState &W = setup_warp(smem_raw, wib, 0u, 0u, c);
-    {
-        const uint32_t *src = reinterpret_cast<const uint32_t *>(plan);
-        uint32_t *dst = reinterpret_cast<uint32_t *>(&P);
-        for (uint32_t w = lane; w < sizeof(DevPlan) / 4; w += 32) dst[w] = src[w];
-        __syncwarp();
-    }
+    WarpState &W = setup_warp(smem_raw, wib, 0u, 0u, 1u, 1u, c);
     const uint32_t k = P.k, last = k - 1;
     while (true) {
         unsigned long long t = 0;
@@ -1754,6 +1776,7 @@ namespace {
 struct LaunchCfg {
     std::vector<DevPlan> dps;
     uint32_t nplans = 0, wpb = 8, threads = 256, tmode = 0, tw = 0, cap = 0, nbufs = 1, heavy_cap = 1;
+    uint32_t ntd = 1, cs = 1;  // tail descriptors and leaf counters per warp (largest plan of the launch)
     size_t smem = 0, blocks = 1, scratch_bytes = 0;
     bool want_stats = false, any_split = false;
     unsigned long long deadline = 0;
@@ -1780,6 +1803,8 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
         d.ntasks = all > d.root_offset ? (all - d.root_offset + stride - 1) / stride : 0;
         total += d.ntasks;
         L.nbufs = std::max(L.nbufs, d.nbufs);
+        L.ntd = std::max(L.ntd, plan_ntd(d));
+        L.cs = std::max(L.cs, plan_cs(d));
         if (d.k > SGE_MAX_K) return fail(SGE_UNSUPPORTED, "plan %u has k=%u", i, d.k);
     }
     // pinned-list tables: a bitmap over all vertices when it fits in 4 KB, else a 512-slot hash
@@ -1794,7 +1819,7 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
         const uint32_t choices[2] = {8, 4};
         for (uint32_t wpb : choices) {
             if (o.warps_per_block && wpb != std::min<uint32_t>(o.warps_per_block, 8)) continue;
-            const size_t smem = warp_smem_bytes(L.tw) * wpb;
+            const size_t smem = warp_smem_bytes(L.tw, L.ntd, L.cs) * wpb;
             int b = 0;
             // static (plan copies) + dynamic shared memory exceed the 48 KB default: opt in
             CUDA_TRY(cudaFuncSetAttribute(count_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1805,7 +1830,7 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
         }
         if (o.warps_per_block && best_warps < 0) {
             L.wpb = std::min<uint32_t>(std::max<uint32_t>(o.warps_per_block, 1), 8);
-            L.smem = warp_smem_bytes(L.tw) * L.wpb;
+            L.smem = warp_smem_bytes(L.tw, L.ntd, L.cs) * L.wpb;
         }
         L.threads = L.wpb * 32;
         CUDA_TRY(cudaFuncSetAttribute(count_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
@@ -1884,11 +1909,11 @@ sge_status enqueue_launch(sge_graph *g, const LaunchCfg &L, unsigned char *B, ui
         if (L.want_stats)
             count_kernel<true><<<(unsigned)L.blocks, L.threads, L.smem, s>>>(
                 dg, dplans, L.nplans, dqueue, dcounts, scratch, L.cap, L.nbufs, L.tw, L.tmode, L.deadline, dflags,
-                dstats, phase, dhcnt, dhids, L.heavy_cap);
+                dstats, phase, dhcnt, dhids, L.heavy_cap, L.ntd, L.cs);
         else
             count_kernel<false><<<(unsigned)L.blocks, L.threads, L.smem, s>>>(
                 dg, dplans, L.nplans, dqueue, dcounts, scratch, L.cap, L.nbufs, L.tw, L.tmode, L.deadline, dflags,
-                dstats, phase, dhcnt, dhids, L.heavy_cap);
+                dstats, phase, dhcnt, dhids, L.heavy_cap, L.ntd, L.cs);
         CUDA_TRY(cudaGetLastError());
         ++launches;
     }
@@ -2149,7 +2174,7 @@ sge_status sge_enumerate(sge_graph *g, const sge_plan *p, uint32_t *d_out, uint6
     d.ntasks = (d.root_kind == SGE_ROOT_ANY) ? 2ull * g->m : g->m;
     d.nbufs = d.k;
     const uint32_t wpb = 8, threads = 256;
-    const size_t smem = warp_smem_bytes(0) * wpb;
+    const size_t smem = warp_smem_bytes(0, 1, 1) * wpb;
     CUDA_TRY(cudaFuncSetAttribute(enum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int bps = 0;
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, enum_kernel, threads, smem));
@@ -2234,7 +2259,6 @@ __global__ void __launch_bounds__(256) count_kernel_noalloc(DevGraph g, const De
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t lane = lane_id();
     const uint32_t wib = threadIdx.x >> 5;
-    DevPlan &P = warp_plan(smem_raw, wib, 0u);
     const size_t gwarp = (size_t)blockIdx.x * (blockDim.x >> 5) + wib;
     Ctx<false> c;
     c.g = g;
@@ -2242,7 +2266,7 @@ __global__ void __launch_bounds__(256) count_kernel_noalloc(DevGraph g, const De
     c.cap = cap;
     c.flags = flags;
     c.set_ops = c.alg_bytes = c.partial = 0;
-    WarpState &W = setup_warp(smem_raw, wib, 0u, 0u, c);  // no pinned tables in this variant
+    WarpState &W = setup_warp(smem_raw, wib, 0u, 0u, SGE_MAX_TAIL, 16u, c);  // no pinned tables in this variant
     c.tstart = 0;
     c.deadline = 0;
     const unsigned long long total = nnz * nplans;
@@ -2258,15 +2282,11 @@ __global__ void __launch_bounds__(256) count_kernel_noalloc(DevGraph g, const De
         for (unsigned long long t = t0; t < t1; ++t) {
             const int pi = (int)(t / nnz);
             if (pi != cur) {
-                if (cur >= 0 && lane == 0 && acc) atomicAdd(counts + cur, acc * P.mult);
+                if (cur >= 0 && lane == 0 && acc) atomicAdd(counts + cur, acc * plans[cur].mult);
                 acc = 0;
                 cur = pi;
-                __syncwarp();
-                const uint32_t *src = reinterpret_cast<const uint32_t *>(plans + cur);
-                uint32_t *dst = reinterpret_cast<uint32_t *>(&P);
-                for (uint32_t w = lane; w < sizeof(DevPlan) / 4; w += 32) dst[w] = src[w];
-                __syncwarp();
             }
+            const DevPlan &P = plans[cur];
             const uint32_t e = (uint32_t)(t - (unsigned long long)pi * nnz);
             const uint32_t u = ub(g.off, g.n + 1, e) - 1;  // source of directed edge e
             const uint32_t v = g.adj[e];
@@ -2275,7 +2295,7 @@ __global__ void __launch_bounds__(256) count_kernel_noalloc(DevGraph g, const De
             acc += run_root<false>(P, W, c, u, v);
         }
     }
-    if (cur >= 0 && lane == 0 && acc) atomicAdd(counts + cur, acc * P.mult);
+    if (cur >= 0 && lane == 0 && acc) atomicAdd(counts + cur, acc * plans[cur].mult);
 }
 
 }  // namespace
@@ -2325,7 +2345,7 @@ extern "C" sge_status sge_count_noalloc(const uint32_t *d_offsets, const uint32_
     const size_t per_warp = (size_t)nbufs * cap * sizeof(uint32_t);
     const size_t avail = SGE_NOALLOC_SCRATCH_BYTES - NOALLOC_LISTS;
     const uint32_t wpb = 8, threads = wpb * 32;
-    const size_t smem = warp_smem_bytes(0) * wpb;
+    const size_t smem = warp_smem_bytes(0, SGE_MAX_TAIL, 16) * wpb;
     size_t max_blocks = avail / (per_warp * wpb);
     if (max_blocks == 0)
         return fail(SGE_UNSUPPORTED,
