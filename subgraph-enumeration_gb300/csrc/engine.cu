@@ -830,8 +830,20 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
         __syncwarp();
         const uint32_t ns = D.nsrc;
         const uint32_t nu = (P.tail_mode == SGE_TAIL_IEP) ? (T - 1 - t) : 0u;
-        // 2. flattened scan: element j belongs to the candidate l with pref[l-1] <= j < pref[l]
+        // 2. flattened scan: element j belongs to the candidate l with
+        // pref[l-1] <= j < pref[l].  A lane's elements of one candidate are
+        // consecutive, so it counts S[{tp}] (and, with one later level,
+        // S[{tp, up}]) in registers and adds them when its candidate changes
         uint32_t l = 0;
+        const uint32_t i0 = (P.tail_mode == SGE_TAIL_CHOOSE) ? 1u : (1u << tp);
+        const uint32_t up1 = nu ? (ord >> (4 * (t + 1))) & 15u : 0u;
+        const uint32_t i1 = i0 | (1u << up1);
+        uint32_t al = 0, a0 = 0, a1 = 0;
+        auto flush = [&]() {
+            if (a0) atomicAdd(&c.cnt[al * c.cs + i0], a0);
+            if (a1) atomicAdd(&c.cnt[al * c.cs + i1], a1);
+            a0 = a1 = 0;
+        };
         for (uint32_t j = lane; j < total; j += 32) {
             while (L.pref[l] <= j) ++l;
             const uint32_t start = l ? L.pref[l - 1] : 0u;
@@ -843,23 +855,26 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
             if (!ok) continue;
             if (P.tail_mode == SGE_TAIL_SINGLE) {
                 ++single;
-            } else if (P.tail_mode == SGE_TAIL_CHOOSE) {
-                atomicAdd(&c.cnt[(l) * c.cs + (1)], 1u);
-            } else {
+                continue;
+            }
+            if (l != al) {
+                flush();
+                al = l;
+            }
+            ++a0;
+            if (nu == 1) {
+                a1 += td_member(c.td[up1], L, W, c, l, y) ? 1u : 0u;
+            } else if (nu > 1) {
                 uint32_t fm = 0;
                 for (uint32_t q = t + 1; q < t + 1 + nu; ++q) {
                     const uint32_t up = (ord >> (4 * q)) & 15u;
                     fm |= (uint32_t)td_member(c.td[up], L, W, c, l, y) << up;
                 }
-                // every subset s of the later positions y belongs to: S[{tp} ∪ s] += 1
-                uint32_t s = fm;
-                while (true) {
-                    atomicAdd(&c.cnt[(l) * c.cs + ((1u << tp) | s)], 1u);
-                    if (s == 0) break;
-                    s = (s - 1) & fm;
-                }
+                // every nonempty subset s of the later positions y belongs to: S[{tp} ∪ s] += 1
+                for (uint32_t sub = fm; sub; sub = (sub - 1) & fm) atomicAdd(&c.cnt[l * c.cs + (i0 | sub)], 1u);
             }
         }
+        if (P.tail_mode != SGE_TAIL_SINGLE) flush();
         __syncwarp();
     }
     // 3. per-candidate results
