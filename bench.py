@@ -236,13 +236,17 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plans", default="", help="comma-separated subset, e.g. house/wcoj-u (profiling)")
     ap.add_argument("--per-plan", action="store_true", help="time each plan alone and print one JSON per plan")
-    ap.add_argument("--workload", default="chunglu7100", choices=["chunglu7100", "batch7"],
-                    help="batch7: 78 random 7-vertex patterns, learned+batched vs plain planning (separate line)")
+    ap.add_argument("--workload", default="chunglu7100", choices=["chunglu7100", "batch7", "ingest"],
+                    help="batch7: 78 random 7-vertex patterns, learned+batched vs plain planning; "
+                         "ingest: R-MAT 2^20 vertices / 16M edges generated and built on the GPU vs the host "
+                         "(separate lines)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch7":
         return run_batch7(args)
+    if args.workload == "ingest":
+        return run_ingest(args)
     world, rank, local = dist_env()
     import torch
     import sge
@@ -353,6 +357,44 @@ def main():
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+INGEST_GRAPH = dict(scale=20, m=16_000_000, a=0.57, b=0.19, c=0.19, seed=11)
+
+
+def run_ingest(args):
+    """Graph ingest for the batch configuration's data graph (R-MAT a=.57
+    b=.19 c=.19, 2^20 vertices, 16M undirected edges): generation, dedup and
+    CSR build on the GPU (sge_graph_create_rmat) against the host generator,
+    host CSR build and upload (sge_gen_rmat + sge_csr_from_edges +
+    sge_graph_create).  Both give the same CSR, which is checked."""
+    import sge
+    import numpy as np
+    gs = INGEST_GRAPH
+    rgs = (gs["scale"], gs["m"], gs["a"], gs["b"], gs["c"], gs["seed"])
+    sge.Engine.rmat_device(10, 5000, seed=1).close()  # context and module load outside the timing
+    dev_s, host_s = [], []
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        eng = sge.Engine.rmat_device(*rgs)
+        dev_s.append(time.perf_counter() - t0)
+        off, nb = eng.graph.offsets, eng.graph.nbrs
+        eng.close()
+    t0 = time.perf_counter()
+    g = sge.gen_rmat(*rgs)
+    hg = sge.Engine(g)
+    host_s.append(time.perf_counter() - t0)
+    hg.close()
+    assert np.array_equal(off, g.offsets) and np.array_equal(nb, g.nbrs)
+    line = {"metric": "R-MAT data graph ingest (generate, dedup, symmetric CSR on the device), seconds",
+            "value": statistics.median(dev_s), "unit": "s", "higher_is_better": False, "n_gpus": 1,
+            "steps": args.steps, "host_s": host_s[0], "speedup_vs_host": host_s[0] / statistics.median(dev_s),
+            "data": "synthetic", "dtype": "u32 ids",
+            "config": {"workload": "rmat_s20_m16M ingest", "graph": dict(gs, generator="rmat"),
+                       "directed_edges": int(nb.size), "csr_identical_to_host": True,
+                       "device_path": "sge_graph_create_rmat (includes the host copy used for planner statistics)",
+                       "host_path": "sge_gen_rmat + sge_csr_from_edges + sge_graph_create (validation, upload)"}}
+    print(json.dumps(line), flush=True)
 
 
 BATCH7_GRAPH = dict(scale=10, m=8000, a=0.57, b=0.19, c=0.19, seed=4)

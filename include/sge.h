@@ -273,6 +273,21 @@ sge_status sge_graph_create(const uint32_t *offsets, const uint32_t *nbrs, uint3
                             uint64_t num_directed_edges, int device, sge_graph **out);
 sge_status sge_graph_destroy(sge_graph *g);
 sge_status sge_graph_get_info(const sge_graph *g, sge_graph_info *info);
+/* ---- device graph ingest (replaces Graph::addDirectedEdges / loadDataGraph's
+ *      CSR build on the host, relation/graph.cpp:143-173,255-419) ----
+ * Builds the symmetric CSR on the GPU from m undirected edges (u,v) held in
+ * device memory on `device` (d_edges: 2m uint32, any order).  Self-loops and
+ * duplicates are dropped; an id >= num_vertices is SGE_BAD_INPUT.  No
+ * counterpart takes device input in the reference. */
+sge_status sge_graph_create_from_device_edges(const uint32_t *d_edges, uint64_t m, uint32_t num_vertices, int device,
+                                              sge_graph **out);
+/* R-MAT generated on the GPU: the graph of sge_gen_rmat's edges for the same
+ * arguments (the same counter-based stream), built as a device graph without
+ * a host round trip of the edges. */
+sge_status sge_graph_create_rmat(uint32_t scale, uint64_t m, uint32_t a_ppm, uint32_t b_ppm, uint32_t c_ppm,
+                                 uint64_t seed, int device, sge_graph **out);
+/* Copies a graph's CSR to host arrays (num_vertices+1 offsets, num_directed_edges neighbours). */
+sge_status sge_graph_copy_csr(const sge_graph *g, uint32_t *offsets, uint32_t *nbrs);
 
 /* ---- compiled plans ---- */
 sge_status sge_plan_create(const sge_plan_blob *blob, sge_plan **out);

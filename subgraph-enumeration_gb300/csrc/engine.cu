@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "common.hpp"
+#include "device_util.hpp"
 
 using namespace sge;
 
@@ -2013,6 +2014,84 @@ sge_status sge_graph_create(const uint32_t *offsets, const uint32_t *nbrs, uint3
         (e = cudaStreamSynchronize(g->stream)) != cudaSuccess)
         return cleanup(fail(SGE_CUDA_ERROR, "graph upload failed: %s", cudaGetErrorString(e)));
     *out = g;
+    return SGE_OK;
+}
+
+}  // extern "C"
+
+namespace {
+// Root edges of a device CSR: directed edge e = (src(e), adj[e]) is a root
+// when adj[e] > src(e); pos[e] is its rank among the roots (CSR order).
+__global__ void root_flags_kernel(const uint32_t *off, const uint32_t *adj, uint32_t n, unsigned long long nnz,
+                                  uint32_t *flags) {
+    const unsigned long long e = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nnz) return;
+    const uint32_t src = ub(off, n + 1, (uint32_t)e) - 1;
+    flags[e] = adj[e] > src ? 1u : 0u;
+}
+__global__ void root_scatter_kernel(const uint32_t *off, const uint32_t *adj, uint32_t n, unsigned long long nnz,
+                                    const uint32_t *flags, const uint32_t *pos, uint2 *edges) {
+    const unsigned long long e = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nnz || !flags[e]) return;
+    const uint32_t src = ub(off, n + 1, (uint32_t)e) - 1;
+    edges[pos[e]] = make_uint2(src, adj[e]);
+}
+}  // namespace
+
+sge_status sge::graph_adopt(uint32_t *d_off, uint32_t *d_adj, uint32_t n, uint64_t nnz, int device,
+                            sge_graph **out) {
+    sge_graph *g = new sge_graph();
+    g->device = device;
+    g->d_off = d_off;
+    g->d_adj = d_adj;
+    g->n = n;
+    g->nnz = nnz;
+    g->m = nnz / 2;
+    auto cleanup = [&](sge_status s) { sge_graph_destroy(g); return s; };
+    cudaError_t e;
+    if ((e = cudaSetDevice(device)) != cudaSuccess) return cleanup(fail(SGE_CUDA_ERROR, "%s", cudaGetErrorString(e)));
+    cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if ((e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreate(&g->ev0)) != cudaSuccess || (e = cudaEventCreate(&g->ev1)) != cudaSuccess)
+        return cleanup(fail(SGE_CUDA_ERROR, "stream/event creation: %s", cudaGetErrorString(e)));
+    if ((e = cudaMalloc(&g->d_edges, sizeof(uint2) * std::max<uint64_t>(g->m, 1))) != cudaSuccess)
+        return cleanup(fail(SGE_OOM, "device allocation of the root edges failed: %s", cudaGetErrorString(e)));
+    if (nnz) {
+        uint32_t *flags = nullptr, *pos = nullptr;
+        if ((e = cudaMalloc(&flags, 4 * nnz)) != cudaSuccess || (e = cudaMalloc(&pos, 4 * nnz)) != cudaSuccess) {
+            cudaFree(flags);
+            return cleanup(fail(SGE_OOM, "root edge scratch: %s", cudaGetErrorString(e)));
+        }
+        const unsigned grid = (unsigned)((nnz + 255) / 256);
+        root_flags_kernel<<<grid, 256, 0, g->stream>>>(d_off, d_adj, n, nnz, flags);
+        sge_status st = device_exclusive_scan(flags, pos, nnz, g->stream);
+        if (st == SGE_OK) {
+            root_scatter_kernel<<<grid, 256, 0, g->stream>>>(d_off, d_adj, n, nnz, flags, pos, g->d_edges);
+            e = cudaStreamSynchronize(g->stream);
+            if (e != cudaSuccess) st = fail(SGE_CUDA_ERROR, "root edges: %s", cudaGetErrorString(e));
+        }
+        cudaFree(flags);
+        cudaFree(pos);
+        if (st != SGE_OK) return cleanup(st);
+    }
+    // planner statistics from a host copy (the same numbers as a host-built graph)
+    std::vector<uint32_t> off((size_t)n + 1), adj(std::max<uint64_t>(nnz, 1));
+    if ((e = cudaMemcpy(off.data(), d_off, 4 * ((size_t)n + 1), cudaMemcpyDeviceToHost)) != cudaSuccess ||
+        (nnz && (e = cudaMemcpy(adj.data(), d_adj, 4 * nnz, cudaMemcpyDeviceToHost)) != cudaSuccess))
+        return cleanup(fail(SGE_CUDA_ERROR, "graph read-back: %s", cudaGetErrorString(e)));
+    for (uint32_t v = 0; v < n; ++v) g->max_deg = std::max(g->max_deg, off[v + 1] - off[v]);
+    sge_graph_stats_compute(off.data(), adj.data(), n, &g->stats);
+    *out = g;
+    return SGE_OK;
+}
+
+extern "C" {
+
+sge_status sge_graph_copy_csr(const sge_graph *g, uint32_t *offsets, uint32_t *nbrs) {
+    if (!g || !offsets || (!nbrs && g->nnz)) return fail(SGE_BAD_INPUT, "sge_graph_copy_csr: null argument");
+    CUDA_TRY(cudaSetDevice(g->device));
+    CUDA_TRY(cudaMemcpy(offsets, g->d_off, 4 * ((size_t)g->n + 1), cudaMemcpyDeviceToHost));
+    if (g->nnz) CUDA_TRY(cudaMemcpy(nbrs, g->d_adj, 4 * g->nnz, cudaMemcpyDeviceToHost));
     return SGE_OK;
 }
 

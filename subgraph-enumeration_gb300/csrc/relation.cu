@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "common.hpp"
+#include "device_util.hpp"
 
 using namespace sge;
 
@@ -213,6 +214,18 @@ sge_status exclusive_scan(const uint32_t *in, uint32_t *out, unsigned long long 
 }
 
 }  // namespace
+
+sge_status sge::device_exclusive_scan(const uint32_t *in, uint32_t *out, uint64_t n, cudaStream_t s) {
+    if (n == 0) return SGE_OK;
+    uint32_t *sums = nullptr;
+    CUDA_TRY(cudaMalloc(&sums, sizeof(uint32_t) * ((n + 1023) / 1024)));
+    sge_status st = exclusive_scan(in, out, n, sums, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    cudaFree(sums);
+    if (st != SGE_OK) return st;
+    if (e != cudaSuccess) return fail(SGE_CUDA_ERROR, "device_exclusive_scan: %s", cudaGetErrorString(e));
+    return SGE_OK;
+}
 
 extern "C" {
 

@@ -129,6 +129,9 @@ SIGNATURES = {
     "sge_graph_create": (C.c_int, [_P(u32), _P(u32), u32, u64, C.c_int, _P(C.c_void_p)]),
     "sge_graph_destroy": (C.c_int, [C.c_void_p]),
     "sge_graph_get_info": (C.c_int, [C.c_void_p, _P(GraphInfo)]),
+    "sge_graph_create_from_device_edges": (C.c_int, [C.c_void_p, u64, u32, C.c_int, _P(C.c_void_p)]),
+    "sge_graph_create_rmat": (C.c_int, [u32, u64, u32, u32, u32, u64, C.c_int, _P(C.c_void_p)]),
+    "sge_graph_copy_csr": (C.c_int, [C.c_void_p, _P(u32), _P(u32)]),
     "sge_plan_create": (C.c_int, [_P(PlanBlob), _P(C.c_void_p)]),
     "sge_plan_destroy": (C.c_int, [C.c_void_p]),
     "sge_count": (C.c_int, [C.c_void_p, _P(C.c_void_p), u32, _P(CountOpts), _P(u64), _P(u64), _P(Stats)]),
@@ -457,6 +460,41 @@ class Engine:
         _check(lib().sge_graph_create(_u32p(self._off), _u32p(self._nb), graph.num_vertices, self._nb.size, device,
                                       C.byref(h)))
         self._h = h
+
+    @classmethod
+    def _adopt(cls, h: C.c_void_p) -> "Engine":
+        eng = cls.__new__(cls)
+        eng._h = h
+        off, nb = eng.csr()
+        eng.graph = DataGraph(off, nb)
+        eng._off, eng._nb = eng.graph.offsets, eng.graph.nbrs
+        return eng
+
+    @classmethod
+    def rmat_device(cls, scale: int, m: int, a: float = 0.57, b: float = 0.19, c: float = 0.19, seed: int = 0,
+                    device: int = 0) -> "Engine":
+        """R-MAT generated and turned into a CSR on the GPU
+        (sge_graph_create_rmat): the same graph as gen_rmat(scale, m, a, b, c, seed)."""
+        h = C.c_void_p()
+        _check(lib().sge_graph_create_rmat(scale, m, round(a * 1e6), round(b * 1e6), round(c * 1e6), seed, device,
+                                           C.byref(h)))
+        return cls._adopt(h)
+
+    @classmethod
+    def from_device_edges(cls, ptr: int, m: int, num_vertices: int, device: int = 0) -> "Engine":
+        """CSR built on the GPU from m undirected (u, v) pairs at device address
+        ptr (sge_graph_create_from_device_edges; self-loops and repeats dropped)."""
+        h = C.c_void_p()
+        _check(lib().sge_graph_create_from_device_edges(C.c_void_p(ptr), m, num_vertices, device, C.byref(h)))
+        return cls._adopt(h)
+
+    def csr(self) -> tuple[np.ndarray, np.ndarray]:
+        """The device CSR copied to host (offsets, neighbours)."""
+        gi = self.info()
+        off = np.zeros(gi["num_vertices"] + 1, np.uint32)
+        nb = np.zeros(max(gi["num_directed_edges"], 1), np.uint32)
+        _check(lib().sge_graph_copy_csr(self._h, _u32p(off), _u32p(nb)))
+        return off, nb[: gi["num_directed_edges"]]
 
     def info(self) -> dict:
         gi = GraphInfo()

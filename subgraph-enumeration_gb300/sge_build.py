@@ -25,7 +25,7 @@ ORACLE_OUT = ORACLE / "_build"
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_SRCS = ["planner.cpp", "graph_io.cpp", "generators.cpp"]
-CU_SRCS = ["engine.cu", "mlp.cu", "relation.cu"]
+CU_SRCS = ["engine.cu", "mlp.cu", "relation.cu", "ingest.cu"]
 
 
 def _run(cmd: list[str], cwd: Path | None = None) -> None:
@@ -43,7 +43,7 @@ def _stale(target: Path, deps: list[Path]) -> bool:
 
 def build_sge(verbose: bool = False) -> Path:
     OUT.mkdir(parents=True, exist_ok=True)
-    headers = [INC / "sge.h", CSRC / "common.hpp"]
+    headers = [INC / "sge.h", CSRC / "common.hpp", CSRC / "device_util.hpp"]
     jobs = []
     objs = []
     for s in CU_SRCS:
