@@ -142,7 +142,7 @@ typedef struct sge_plan_opts {
 /* Execution options */
 typedef struct sge_count_opts {
     uint32_t blocks_per_sm;     /* 0 = occupancy-derived */
-    uint32_t warps_per_block;   /* 0 = default (8) */
+    uint32_t warps_per_block;   /* 0 = occupancy-derived (at most 4) */
     uint32_t chunk;             /* root tasks per queue grab; 0 = auto */
     double   time_budget_s;     /* 0 = unlimited; otherwise kernels stop and report SGE_TIMEOUT */
     uint32_t max_level_capacity;/* 0 = graph max degree; smaller values exercise the overflow path */

@@ -100,7 +100,6 @@ struct WarpState {
     uint32_t fcnt[SGE_MAX_K];
     const uint32_t *lptr[SGE_MAX_K];      // N(m[j]) of the matched levels
     uint32_t llen[SGE_MAX_K];
-    uint32_t vslot[SGE_MAX_VSLOTS];       // exploration: length of the version list in each buffer slot
     uint32_t pmode[3];                    // pinned N(m[0]), N(m[1]), level-2 list: 0 none, 1 bitmap, 2 hash
     uint32_t hcnt[SGE_MAX_K];             // hoisted tail lists (buffer slot = level)
     uint32_t hpin;                        // tail level whose hoisted list is pinned in table 2 (0 = none)
@@ -123,7 +122,7 @@ struct TailDesc {
 // level, each with its own matched values for the levels from L0 on.
 struct LeafState {
     uint32_t cm[32][2];
-    const uint32_t *cptr[32][2];
+    uint32_t coff[32][2];  // CSR offset of each candidate's own lists (slot 0/1)
     uint32_t clen[32][2];
     const uint32_t *bptr[32];
     uint32_t pref[32];
@@ -141,12 +140,12 @@ struct PairState {
     uint32_t exv[SGE_MAX_K];          // matched values below a that level a+1 excludes
     uint32_t nex;
     uint32_t x[32];                   // this batch's level-a candidates
-    const uint32_t *xp[32];           // N(x)
+    uint32_t xo[32];                  // N(x): CSR offset
     uint32_t xl[32];
     const uint32_t *bp[32];           // list scanned for candidate x (trimmed by bounds)
     uint32_t pref[32];
     uint32_t qx[64], qy[64];          // (x, y) pairs waiting for the leaf
-    uint32_t tr[32], tlo[32], thi[32];  // inline tail: count for x before y's own exclusion, x's range
+    uint32_t tr[32];                  // inline tail: x's count before y's own exclusion
     TailDesc ptd;                     // inline tail: the tail level as seen from level a
 };
 
@@ -228,6 +227,12 @@ __device__ __forceinline__ void nbr(const DevGraph &g, uint32_t v, const uint32_
     len = b - a;
 }
 
+__device__ __forceinline__ void nbr_off(const DevGraph &g, uint32_t v, uint32_t &off, uint32_t &len) {
+    const uint32_t a = __ldg(g.off + v), b = __ldg(g.off + v + 1);
+    off = a;
+    len = b - a;
+}
+
 // Trim a sorted list to (lo, hi).
 __device__ __forceinline__ void trim(const uint32_t *&p, uint32_t &len, const Bounds &b) {
     if (b.has_lo) { uint32_t s = ub(p, len, b.lo); p += s; len -= s; }
@@ -246,6 +251,7 @@ struct Ctx {
     LeafState *L;
     PairState *PS;
     TailDesc *td;     // this warp's tail descriptors (one per inclusion–exclusion pass)
+    uint32_t *vs;     // exploration: length of the version list in each buffer slot
     uint32_t *cnt;    // per-candidate counters S[subset]: cnt[l * cs + subset]
     uint32_t cs;
     unsigned long long tstart, deadline;  // globaltimer of the warp's start; budget in ns (0 = none)
@@ -331,9 +337,11 @@ __device__ void pin_root(const DevPlan &P, WarpState &W, Ctx<STATS> &c) {
 
 // Exploration: version (j, i) list length and pointer.  The first parent's
 // version is N(m[j]) itself; the others live in buffer slot[j][i].
-__device__ __forceinline__ uint32_t version_len(const DevPlan &P, const WarpState &W, uint32_t j, uint32_t i) {
+template <bool STATS>
+__device__ __forceinline__ uint32_t version_len(const DevPlan &P, const WarpState &W, const Ctx<STATS> &c, uint32_t j,
+                                                uint32_t i) {
     const int s = P.slot[j][i];
-    return s < 0 ? W.llen[j] : W.vslot[s];
+    return s < 0 ? W.llen[j] : c.vs[s];
 }
 
 template <bool STATS>
@@ -350,7 +358,7 @@ __device__ void unpin_root(const DevPlan &P, WarpState &W, Ctx<STATS> &c) {
         if (W.pmode[j]) unpin_list(W, c, j, W.lptr[j], W.llen[j]);
     if (W.pmode[2]) {
         if (W.hpin && P.join_style == SGE_JOIN_EXPLORATION)
-            unpin_list(W, c, 2, version_ptr(P, W, c, 1, W.hpin), version_len(P, W, 1, W.hpin));
+            unpin_list(W, c, 2, version_ptr(P, W, c, 1, W.hpin), version_len(P, W, c, 1, W.hpin));
         else if (W.hpin) unpin_list(W, c, 2, c.buf + (size_t)W.hpin * c.cap, W.hcnt[W.hpin]);
         else unpin_list(W, c, 2, W.flist[2], W.fcnt[2]);
     }
@@ -530,7 +538,7 @@ __device__ __forceinline__ bool explore_update(const DevPlan &P, WarpState &W, C
         }
         uint32_t pj = 31 - __clz(below);  // previous parent of i
         const uint32_t *prev = version_ptr(P, W, c, pj, i);
-        uint32_t plen = version_len(P, W, pj, i);
+        uint32_t plen = version_len(P, W, c, pj, i);
         uint32_t *out = c.buf + (size_t)P.slot[j][i] * c.cap;
         if (STATS) { c.set_ops += 1; c.alg_bytes += 8ull + 4ull * (plen + W.llen[j]); }
         uint32_t total = 0;
@@ -550,7 +558,7 @@ __device__ __forceinline__ bool explore_update(const DevPlan &P, WarpState &W, C
             total += __popc(bal);
         }
         __syncwarp();
-        if (lane == 0) W.vslot[P.slot[j][i]] = total;
+        if (lane == 0) c.vs[P.slot[j][i]] = total;
         __syncwarp();
         if (total > c.cap) {
             if (lane == 0) atomicOr(c.flags, FLAG_OVERFLOW);
@@ -566,7 +574,7 @@ template <bool STATS>
 __device__ __forceinline__ void explore_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32_t i) {
     uint32_t lastp = 31 - __clz(P.parents[i]);
     const uint32_t *bp = version_ptr(P, W, c, lastp, i);
-    uint32_t blen = version_len(P, W, lastp, i);
+    uint32_t blen = version_len(P, W, c, lastp, i);
     Bounds b = level_bounds(P, W, i);
     __syncwarp();
     if (lane_id() == 0) { W.flist[i] = bp; W.fcnt[i] = blen; }
@@ -611,8 +619,8 @@ __device__ __forceinline__ void for_tail_lists(const DevPlan &P, const WarpState
         if (P.slot[lastp][i] < 0 && lastp < 2 && W.pmode[lastp]) {
             if (!f(W.lptr[lastp], W.llen[lastp], (int)lastp, true)) return;
         } else if (lastp == 1 && W.hpin == i) {
-            if (!f(version_ptr(P, W, c, 1, i), version_len(P, W, 1, i), SRC_HOISTED, true)) return;
-        } else if (!f(version_ptr(P, W, c, lastp, i), version_len(P, W, lastp, i), -1, false)) {
+            if (!f(version_ptr(P, W, c, 1, i), version_len(P, W, c, 1, i), SRC_HOISTED, true)) return;
+        } else if (!f(version_ptr(P, W, c, lastp, i), version_len(P, W, c, lastp, i), -1, false)) {
             return;
         }
         shared = 0;
@@ -633,7 +641,7 @@ __device__ __forceinline__ void for_tail_lists(const DevPlan &P, const WarpState
     }
     for (uint32_t msk = cand; msk; msk &= msk - 1) {
         const uint32_t j = __ffs(msk) - 1;
-        if (!f(L.cptr[l][j - lc.L0], L.clen[l][j - lc.L0], (int)j, false)) return;
+        if (!f(c.g.adj + L.coff[l][j - lc.L0], L.clen[l][j - lc.L0], (int)j, false)) return;
     }
 }
 
@@ -653,8 +661,9 @@ __device__ __forceinline__ Bounds td_bounds(const TailDesc &D, const LeafState &
     return b;
 }
 
-__device__ __forceinline__ const uint32_t *td_ptr(const TailDesc &D, const LeafState &L, uint32_t q, uint32_t l) {
-    return D.kind[q] >= 4 ? L.cptr[l][D.kind[q] - 4] : D.ptr[q];
+__device__ __forceinline__ const uint32_t *td_ptr(const TailDesc &D, const LeafState &L, const uint32_t *adj,
+                                                  uint32_t q, uint32_t l) {
+    return D.kind[q] >= 4 ? adj + L.coff[l][D.kind[q] - 4] : D.ptr[q];
 }
 __device__ __forceinline__ uint32_t td_len(const TailDesc &D, const LeafState &L, uint32_t q, uint32_t l) {
     return D.kind[q] >= 4 ? L.clen[l][D.kind[q] - 4] : D.len[q];
@@ -667,7 +676,7 @@ __device__ __forceinline__ bool td_has(const TailDesc &D, const LeafState &L, co
     const uint32_t k = D.kind[q];
     if (k < 3) return pin_has(c.tab + k * c.tw, W.pmode[k], c.tw, y);
     if (k == 3) return contains(D.ptr[q], D.len[q], y);
-    return contains(L.cptr[l][k - 4], L.clen[l][k - 4], y);
+    return contains(c.g.adj + L.coff[l][k - 4], L.clen[l][k - 4], y);
 }
 
 __device__ __forceinline__ bool td_excluded(const TailDesc &D, const LeafState &L, uint32_t l, uint32_t y) {
@@ -770,7 +779,7 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
         const bool direct = (P.tail_mode != SGE_TAIL_IEP || t + 1 == T) && D.nsrc == 1;
         if (direct) {
             if (lane < ncand) {
-                const uint32_t *fp = td_ptr(D, L, 0, lane);
+                const uint32_t *fp = td_ptr(D, L, c.g.adj, 0, lane);
                 const uint32_t fl = td_len(D, L, 0, lane);
                 const Bounds b = td_bounds(D, L, lane);
                 const uint32_t *bp = fp;
@@ -815,7 +824,7 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
         const uint32_t *bp = nullptr;
         uint32_t blen = 0;
         if (lane < ncand) {
-            bp = td_ptr(D, L, bq, lane);
+            bp = td_ptr(D, L, c.g.adj, bq, lane);
             blen = td_len(D, L, bq, lane);
             trim(bp, blen, td_bounds(D, L, lane));
         }
@@ -911,8 +920,8 @@ __device__ unsigned long long leaf_roots(const DevPlan &P, WarpState &W, Ctx<STA
     if (lane < n) {
         L.cm[lane][0] = u;
         L.cm[lane][1] = v;
-        nbr(c.g, u, L.cptr[lane][0], L.clen[lane][0]);
-        nbr(c.g, v, L.cptr[lane][1], L.clen[lane][1]);
+        nbr_off(c.g, u, L.coff[lane][0], L.clen[lane][0]);
+        nbr_off(c.g, v, L.coff[lane][1], L.clen[lane][1]);
     }
     __syncwarp();
     return leaf_chunk(P, W, c, 0, n);
@@ -930,8 +939,8 @@ __device__ __forceinline__ unsigned long long pair_flush(const DevPlan &P, WarpS
         const uint32_t x = S.qx[lane], y = S.qy[lane];
         L.cm[lane][0] = x;
         L.cm[lane][1] = y;
-        if ((P.tail_par >> a) & 1u) nbr(c.g, x, L.cptr[lane][0], L.clen[lane][0]);
-        if ((P.tail_par >> (a + 1)) & 1u) nbr(c.g, y, L.cptr[lane][1], L.clen[lane][1]);
+        if ((P.tail_par >> a) & 1u) nbr_off(c.g, x, L.coff[lane][0], L.clen[lane][0]);
+        if ((P.tail_par >> (a + 1)) & 1u) nbr_off(c.g, y, L.coff[lane][1], L.clen[lane][1]);
     }
     __syncwarp();
     return leaf_chunk(P, W, c, a, nq);
@@ -954,7 +963,7 @@ __device__ __forceinline__ void pair_sources(const DevPlan &P, const WarpState &
                 if (P.slot[lastp][i] < 0 && lastp < 2 && W.pmode[lastp]) {
                     S.sptr[ns] = W.lptr[lastp]; S.slen[ns] = W.llen[lastp]; S.stab[ns] = (int32_t)lastp;
                 } else {
-                    S.sptr[ns] = version_ptr(P, W, c, lastp, i); S.slen[ns] = version_len(P, W, lastp, i); S.stab[ns] = -1;
+                    S.sptr[ns] = version_ptr(P, W, c, lastp, i); S.slen[ns] = version_len(P, W, c, lastp, i); S.stab[ns] = -1;
                 }
                 ++ns;
             }
@@ -990,7 +999,7 @@ __device__ __forceinline__ void pair_sources(const DevPlan &P, const WarpState &
 template <bool STATS>
 __device__ __forceinline__ bool pair_in(const WarpState &W, const Ctx<STATS> &c, const PairState &S, int q,
                                         uint32_t l, uint32_t y) {
-    if (q < 0) return contains(S.xp[l], S.xl[l], y);
+    if (q < 0) return contains(c.g.adj + S.xo[l], S.xl[l], y);
     if (S.stab[q] >= 0) return pin_has(c.tab + S.stab[q] * c.tw, W.pmode[S.stab[q]], c.tw, y);
     return contains(S.sptr[q], S.slen[q], y);
 }
@@ -1003,7 +1012,7 @@ __device__ __forceinline__ bool pair_tail_has(const WarpState &W, const Ctx<STAT
     const uint32_t k = D.kind[0];
     if (k < 3) return pin_has(c.tab + k * c.tw, W.pmode[k], c.tw, v);
     if (k == 3) return contains(D.ptr[0], D.len[0], v);
-    return contains(S.xp[l], S.xl[l], v);
+    return contains(c.g.adj + S.xo[l], S.xl[l], v);
 }
 
 // The last two enumerated levels as one step: for 32 candidates x of level
@@ -1061,7 +1070,7 @@ __device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32
         if (lane < nc) {
             x = S.x[lane];
             nbr(c.g, x, xp, xl);
-            S.xp[lane] = xp;
+            S.xo[lane] = (uint32_t)(xp - c.g.adj);
             S.xl[lane] = xl;
         }
         {
@@ -1126,8 +1135,6 @@ __device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32
                         --cnt;
                 }
                 S.tr[lane] = cnt;
-                S.tlo[lane] = tb.has_lo ? tb.lo : 0u;
-                S.thi[lane] = tb.has_hi ? tb.hi : 0xFFFFFFFFu;
                 if (STATS) c.alg_bytes += 4ull * (2u + D.nex) * (31u - __clz(fl + 1u));
             }
         }
@@ -1161,7 +1168,10 @@ __device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32
                 if (keep) {
                     uint32_t r = S.tr[l];
                     // y itself, when the tail excludes it and it lies in x's range and list
-                    if ((D.ex_slots & 2u) && (!D.has_lo || y > S.tlo[l]) && (!D.has_hi || y < S.thi[l]) &&
+                    const uint32_t xl0 = S.x[l];
+                    const uint32_t tlo = (D.lo_slots & 1u) ? max(D.lo, xl0) : D.lo;
+                    const uint32_t thi = (D.hi_slots & 1u) ? min(D.hi, xl0) : D.hi;
+                    if ((D.ex_slots & 2u) && (!D.has_lo || y > tlo) && (!D.has_hi || y < thi) &&
                         pair_tail_has(W, c, S, l, y))
                         --r;
                     isum += r;
@@ -1232,7 +1242,7 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
     if (explore) {
         ok = explore_update(P, W, c, 0) && explore_update(P, W, c, 1);
         if (ok && P.epin && c.tmode && W.pmode[2] == 0u) {
-            pin_list(W, c, 2, version_ptr(P, W, c, 1, P.epin), version_len(P, W, 1, P.epin));
+            pin_list(W, c, 2, version_ptr(P, W, c, 1, P.epin), version_len(P, W, c, 1, P.epin));
             __syncwarp();
             if (lane == 0 && W.pmode[2]) W.hpin = P.epin;
             __syncwarp();
@@ -1276,7 +1286,7 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
                 if (valid) {
                     const uint32_t rk = __popc(bal & ((1u << lane) - 1u));
                     L.cm[rk][0] = x;
-                    if ((P.tail_par >> L0) & 1u) nbr(c.g, x, L.cptr[rk][0], L.clen[rk][0]);
+                    if ((P.tail_par >> L0) & 1u) nbr_off(c.g, x, L.coff[rk][0], L.clen[rk][0]);
                 }
                 __syncwarp();
                 if (nc) acc += leaf_chunk(P, W, c, L0, nc);
@@ -1318,16 +1328,16 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
 // plans themselves stay in global memory (read through L1): the fewer bytes a
 // warp holds, the more warps are resident, and the DFS is latency-bound.
 __host__ __device__ constexpr size_t align128(size_t x) { return (x + 127) & ~(size_t)127; }
-__host__ __device__ inline size_t warp_smem_bytes(uint32_t tw, uint32_t ntd, uint32_t cs) {
+__host__ __device__ inline size_t warp_smem_bytes(uint32_t tw, uint32_t ntd, uint32_t cs, uint32_t nvs) {
     return align128(sizeof(WarpState)) + align128(sizeof(LeafState)) + align128(sizeof(PairState)) +
            align128(ntd * sizeof(TailDesc)) + align128(32ull * cs * sizeof(uint32_t)) +
-           align128(3ull * tw * sizeof(uint32_t));
+           align128(nvs * sizeof(uint32_t)) + align128(3ull * tw * sizeof(uint32_t));
 }
 
 template <bool STATS>
 __device__ __forceinline__ WarpState &setup_warp(unsigned char *smem, uint32_t wib, uint32_t tw, uint32_t tmode,
-                                                 uint32_t ntd, uint32_t cs, Ctx<STATS> &c) {
-    unsigned char *base = smem + (size_t)wib * warp_smem_bytes(tw, ntd, cs);
+                                                 uint32_t ntd, uint32_t cs, uint32_t nvs, Ctx<STATS> &c) {
+    unsigned char *base = smem + (size_t)wib * warp_smem_bytes(tw, ntd, cs, nvs);
     WarpState &W = *reinterpret_cast<WarpState *>(base);
     base += align128(sizeof(WarpState));
     c.L = reinterpret_cast<LeafState *>(base);
@@ -1339,6 +1349,8 @@ __device__ __forceinline__ WarpState &setup_warp(unsigned char *smem, uint32_t w
     c.cnt = reinterpret_cast<uint32_t *>(base);
     c.cs = cs;
     base += align128(32ull * cs * sizeof(uint32_t));
+    c.vs = reinterpret_cast<uint32_t *>(base);
+    base += align128(nvs * sizeof(uint32_t));
     c.tab = reinterpret_cast<uint32_t *>(base);
     c.tw = tw;
     c.tmode = tmode;
@@ -1351,6 +1363,9 @@ __device__ __forceinline__ WarpState &setup_warp(unsigned char *smem, uint32_t w
 
 // Tail descriptors and counters one plan's leaf needs.
 __host__ __device__ inline uint32_t plan_ntd(const DevPlan &d) { return d.tail_mode == SGE_TAIL_IEP ? d.T : 1u; }
+__host__ __device__ inline uint32_t plan_nvs(const DevPlan &d) {
+    return d.join_style == SGE_JOIN_EXPLORATION ? d.nbufs : 1u;
+}
 __host__ __device__ inline uint32_t plan_cs(const DevPlan &d) {
     return d.tail_mode == SGE_TAIL_IEP ? (1u << d.T) : (d.tail_mode == SGE_TAIL_CHOOSE ? 2u : 1u);
 }
@@ -1382,14 +1397,18 @@ __device__ __forceinline__ uint32_t level2_bound(const DevGraph &g, const DevPla
 // split_H is appended to its plan's heavy list (while there is room) instead.
 // Phase 1 runs the heavy roots as split_C tasks each, task c covering level-2
 // candidates [c·S, (c+1)·S); tasks past a root's bound end at once.
+// 4-warp blocks, 7 per SM: 72 registers per thread and ~8 KB of shared
+// memory per warp fit 28 resident warps (the DFS is latency-bound, so
+// resident warps set the speed)
+constexpr uint32_t COUNT_MAX_WARPS = 4;
 template <bool STATS>
-__global__ void __launch_bounds__(256, 3) count_kernel(DevGraph g, const DevPlan *__restrict__ plans, uint32_t nplans,
+__global__ void __launch_bounds__(COUNT_MAX_WARPS * 32, 7) count_kernel(DevGraph g, const DevPlan *__restrict__ plans, uint32_t nplans,
                                                     unsigned long long *queues, unsigned long long *counts,
                                                     uint32_t *scratch, uint32_t cap, uint32_t bufs_per_warp,
                                                     uint32_t tw, uint32_t tmode, unsigned long long deadline_ns,
                                                     uint32_t *flags, DevStats *stats, uint32_t phase,
                                                     uint32_t *heavy_cnt, uint32_t *heavy_ids, uint32_t heavy_cap,
-                                                    uint32_t ntd, uint32_t cs) {
+                                                    uint32_t ntd, uint32_t cs, uint32_t nvs) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t lane = lane_id();
     const uint32_t wib = threadIdx.x >> 5;
@@ -1400,7 +1419,7 @@ __global__ void __launch_bounds__(256, 3) count_kernel(DevGraph g, const DevPlan
     c.cap = cap;
     c.flags = flags;
     c.set_ops = c.alg_bytes = c.partial = 0;
-    WarpState &W = setup_warp(smem_raw, wib, tw, tmode, ntd, cs, c);
+    WarpState &W = setup_warp(smem_raw, wib, tw, tmode, ntd, cs, nvs, c);
     unsigned long long roots = 0;
     unsigned long long tstart = 0;
     if (lane == 0) tstart = globaltimer_ns();
@@ -1499,7 +1518,7 @@ __global__ void __launch_bounds__(256) enum_kernel(DevGraph g, const DevPlan *__
     c.set_ops = c.alg_bytes = c.partial = 0;
     c.tstart = 0;
     c.deadline = 0;
-    WarpState &W = setup_warp(smem_raw, wib, 0u, 0u, 1u, 1u, c);
+    WarpState &W = setup_warp(smem_raw, wib, 0u, 0u, 1u, 1u, SGE_MAX_VSLOTS, c);
     const uint32_t k = P.k, last = k - 1;
     while (true) {
         unsigned long long t = 0;
@@ -1792,7 +1811,7 @@ namespace {
 struct LaunchCfg {
     std::vector<DevPlan> dps;
     uint32_t nplans = 0, wpb = 8, threads = 256, tmode = 0, tw = 0, cap = 0, nbufs = 1, heavy_cap = 1;
-    uint32_t ntd = 1, cs = 1;  // tail descriptors and leaf counters per warp (largest plan of the launch)
+    uint32_t ntd = 1, cs = 1, nvs = 1;  // per-warp tail descriptors, leaf counters, version slots (largest plan)
     size_t smem = 0, blocks = 1, scratch_bytes = 0;
     bool want_stats = false, any_split = false;
     unsigned long long deadline = 0;
@@ -1821,21 +1840,22 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
         L.nbufs = std::max(L.nbufs, d.nbufs);
         L.ntd = std::max(L.ntd, plan_ntd(d));
         L.cs = std::max(L.cs, plan_cs(d));
+        L.nvs = std::max(L.nvs, plan_nvs(d));
         if (d.k > SGE_MAX_K) return fail(SGE_UNSUPPORTED, "plan %u has k=%u", i, d.k);
     }
     // pinned-list tables: a bitmap over all vertices when it fits in 4 KB, else a 512-slot hash
     if (g->n <= 32768u) { L.tmode = 1; L.tw = std::max<uint32_t>(32u, ((g->n + 31u) / 32u + 31u) & ~31u); }
     else { L.tmode = 2; L.tw = 512; }
     L.want_stats = o.collect_counters != 0;
-    // warps per block: 8 or 4, whichever keeps more warps resident per SM
+    // warps per block: 4 or 2, whichever keeps more warps resident per SM
     // (shared memory per warp is several KB, so smaller blocks pack better)
     int bps = 0;
     {
         int best_warps = -1;
-        const uint32_t choices[2] = {8, 4};
+        const uint32_t choices[2] = {COUNT_MAX_WARPS, 2};
         for (uint32_t wpb : choices) {
-            if (o.warps_per_block && wpb != std::min<uint32_t>(o.warps_per_block, 8)) continue;
-            const size_t smem = warp_smem_bytes(L.tw, L.ntd, L.cs) * wpb;
+            if (o.warps_per_block && wpb != std::min<uint32_t>(o.warps_per_block, COUNT_MAX_WARPS)) continue;
+            const size_t smem = warp_smem_bytes(L.tw, L.ntd, L.cs, L.nvs) * wpb;
             int b = 0;
             // static (plan copies) + dynamic shared memory exceed the 48 KB default: opt in
             CUDA_TRY(cudaFuncSetAttribute(count_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1845,8 +1865,8 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
             if (b * (int)wpb > best_warps) { best_warps = b * (int)wpb; bps = b; L.wpb = wpb; L.smem = smem; }
         }
         if (o.warps_per_block && best_warps < 0) {
-            L.wpb = std::min<uint32_t>(std::max<uint32_t>(o.warps_per_block, 1), 8);
-            L.smem = warp_smem_bytes(L.tw, L.ntd, L.cs) * L.wpb;
+            L.wpb = std::min<uint32_t>(std::max<uint32_t>(o.warps_per_block, 1), COUNT_MAX_WARPS);
+            L.smem = warp_smem_bytes(L.tw, L.ntd, L.cs, L.nvs) * L.wpb;
         }
         L.threads = L.wpb * 32;
         CUDA_TRY(cudaFuncSetAttribute(count_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
@@ -1925,11 +1945,11 @@ sge_status enqueue_launch(sge_graph *g, const LaunchCfg &L, unsigned char *B, ui
         if (L.want_stats)
             count_kernel<true><<<(unsigned)L.blocks, L.threads, L.smem, s>>>(
                 dg, dplans, L.nplans, dqueue, dcounts, scratch, L.cap, L.nbufs, L.tw, L.tmode, L.deadline, dflags,
-                dstats, phase, dhcnt, dhids, L.heavy_cap, L.ntd, L.cs);
+                dstats, phase, dhcnt, dhids, L.heavy_cap, L.ntd, L.cs, L.nvs);
         else
             count_kernel<false><<<(unsigned)L.blocks, L.threads, L.smem, s>>>(
                 dg, dplans, L.nplans, dqueue, dcounts, scratch, L.cap, L.nbufs, L.tw, L.tmode, L.deadline, dflags,
-                dstats, phase, dhcnt, dhids, L.heavy_cap, L.ntd, L.cs);
+                dstats, phase, dhcnt, dhids, L.heavy_cap, L.ntd, L.cs, L.nvs);
         CUDA_TRY(cudaGetLastError());
         ++launches;
     }
@@ -2268,7 +2288,7 @@ sge_status sge_enumerate(sge_graph *g, const sge_plan *p, uint32_t *d_out, uint6
     d.ntasks = (d.root_kind == SGE_ROOT_ANY) ? 2ull * g->m : g->m;
     d.nbufs = d.k;
     const uint32_t wpb = 8, threads = 256;
-    const size_t smem = warp_smem_bytes(0, 1, 1) * wpb;
+    const size_t smem = warp_smem_bytes(0, 1, 1, SGE_MAX_VSLOTS) * wpb;
     CUDA_TRY(cudaFuncSetAttribute(enum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int bps = 0;
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, enum_kernel, threads, smem));
@@ -2360,7 +2380,7 @@ __global__ void __launch_bounds__(256) count_kernel_noalloc(DevGraph g, const De
     c.cap = cap;
     c.flags = flags;
     c.set_ops = c.alg_bytes = c.partial = 0;
-    WarpState &W = setup_warp(smem_raw, wib, 0u, 0u, SGE_MAX_TAIL, 16u, c);  // no pinned tables in this variant
+    WarpState &W = setup_warp(smem_raw, wib, 0u, 0u, SGE_MAX_TAIL, 16u, SGE_MAX_VSLOTS, c);  // no pinned tables here
     c.tstart = 0;
     c.deadline = 0;
     const unsigned long long total = nnz * nplans;
@@ -2439,7 +2459,7 @@ extern "C" sge_status sge_count_noalloc(const uint32_t *d_offsets, const uint32_
     const size_t per_warp = (size_t)nbufs * cap * sizeof(uint32_t);
     const size_t avail = SGE_NOALLOC_SCRATCH_BYTES - NOALLOC_LISTS;
     const uint32_t wpb = 8, threads = wpb * 32;
-    const size_t smem = warp_smem_bytes(0, SGE_MAX_TAIL, 16) * wpb;
+    const size_t smem = warp_smem_bytes(0, SGE_MAX_TAIL, 16, SGE_MAX_VSLOTS) * wpb;
     size_t max_blocks = avail / (per_warp * wpb);
     if (max_blocks == 0)
         return fail(SGE_UNSUPPORTED,
