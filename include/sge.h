@@ -150,7 +150,8 @@ typedef struct sge_count_opts {
     uint64_t root_offset;       /* (root-range sharding across ranks, or sampled runs) */
     uint32_t collect_counters;  /* 1: run the instrumented kernel (set_ops, alg_bytes, partial matches) */
     uint32_t heavy_threshold;   /* 0 = auto; otherwise roots whose level-2 list may exceed it are split
-                                   into tasks of 128 level-2 candidates run by a second launch */
+                                   into tasks of level-2 candidates (128 at four enumerated levels, a
+                                   quarter as many per extra level) run by a second launch */
 } sge_count_opts;
 
 /* Statistics of one sge_count call (per call, summed over plans).  kernel_ms,
@@ -264,6 +265,19 @@ sge_status sge_mlp_train(sge_mlp *m, const float *x, const float *t, uint32_t n,
 sge_status sge_plan_pattern_learned(uint32_t k, uint32_t m, const uint32_t *edges, const sge_graph_stats *stats,
                                     const sge_plan_opts *opts, sge_mlp *scorer, uint32_t shortlist,
                                     sge_plan_blob *out);
+
+/* Plans with GPU root sampling (the sampled-cardinality cost slot of
+ * optCostOrder / cardEstimateUnlabeled, plan/optimizer.cpp:441-577,
+ * plan/estimator.cpp:562-661): the cost model's best `shortlist` candidates
+ * (0 = 8) each count the root sample t ≡ 0 (mod sample_stride) on g with the
+ * instrumented kernel, and the least sampled work (algorithmic bytes + 64 B
+ * per set operation) wins.  A candidate is cut off past 0.5 s or four times
+ * the fastest sample; if all are, the cost model's choice stands.  sampled_ms
+ * (may be NULL; shortlist entries) receives each sample's time, -1 when cut
+ * off or absent. */
+sge_status sge_plan_pattern_sampled(uint32_t k, uint32_t m, const uint32_t *edges, sge_graph *g,
+                                    const sge_plan_opts *opts, uint32_t shortlist, uint64_t sample_stride,
+                                    sge_plan_blob *out, double *sampled_ms);
 
 /* Check a plan blob for internal consistency (levels, masks, tail validity). */
 sge_status sge_plan_validate(const sge_plan_blob *blob);

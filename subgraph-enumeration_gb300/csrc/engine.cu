@@ -1600,6 +1600,7 @@ struct sge_graph {
     size_t batch_bytes = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int num_sms = 0;
+    bool launched = false;     // a counting launch has run on this graph
 };
 
 struct sge_plan {
@@ -1892,11 +1893,15 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
     // share of the launch is about ntasks × (mean endpoint degree M2/M1) /
     // warps candidates; roots are split only when one could exceed a quarter
     // of that share (splitting repeats the root's setup in every task)
-    const uint32_t split_S = 128;
     unsigned long long max_tasks = 1;
     const unsigned long long warps = blocks * L.wpb;
     const double mean_deg = g->stats.moments[1] > 0 ? g->stats.moments[2] / g->stats.moments[1] : 1.0;
     for (auto &d : L.dps) {
+        // deeper plans do more work per level-2 candidate (and far more under
+        // a hub), so their tasks hold fewer candidates: 128 at four
+        // enumerated levels, a quarter as many per extra level
+        const uint32_t deep = d.ne > 4 ? std::min<uint32_t>(d.ne - 4, 3u) : 0u;
+        const uint32_t split_S = std::max<uint32_t>(128u >> (2 * deep), 2u);
         const double share = (double)d.ntasks * mean_deg / (double)std::max<unsigned long long>(warps, 1);
         const uint32_t split_H = o.heavy_threshold ? std::max(o.heavy_threshold, split_S)
                                                    : (uint32_t)std::min(1e9, std::max(4.0 * split_S, share / 4.0));
@@ -2174,6 +2179,7 @@ sge_status sge_count(sge_graph *g, const sge_plan *const *plans, uint32_t nplans
     CUDA_TRY(cudaEventRecord(g->ev0, g->stream));
     uint32_t launches = 0;
     if ((st = enqueue_launch(g, L, B, g->d_scratch, g->stream, launches)) != SGE_OK) return st;
+    g->launched = true;
     CUDA_TRY(cudaEventRecord(g->ev1, g->stream));
     std::vector<unsigned long long> hc(nplans);
     uint32_t hflags = 0;
@@ -2185,6 +2191,52 @@ sge_status sge_count(sge_graph *g, const sge_plan *const *plans, uint32_t nplans
     float ms = 0;
     cudaEventElapsedTime(&ms, g->ev0, g->ev1);
     return finish_counts(L, hc.data(), hflags, hs, ms, launches, t_start, plans, counts, instances, stats, o);
+}
+
+// GPU root sampling as the planner's cost: each shortlisted candidate counts
+// one residue class of the root tasks with the instrumented kernel, and the
+// candidate with the least sampled work (algorithmic bytes + 64 B per set
+// operation) wins.  Work, not time: a sample's time is set by its slowest
+// root, its work by all of them.  A candidate is cut off past 0.5 s, or past
+// four times the fastest sample so far; when every candidate is cut off the
+// cost model's choice stands.
+sge_status sge_plan_pattern_sampled(uint32_t k, uint32_t m, const uint32_t *edges, sge_graph *g,
+                                    const sge_plan_opts *opts, uint32_t shortlist, uint64_t sample_stride,
+                                    sge_plan_blob *out, double *sampled_ms) {
+    if (!g || !out || !edges) return fail(SGE_BAD_INPUT, "sge_plan_pattern_sampled: null argument");
+    if (shortlist == 0) shortlist = 8;
+    std::vector<sge_plan_blob> cands(shortlist);
+    uint32_t n = 0;
+    sge_status st = sge_plan_candidates(k, m, edges, &g->stats, opts, cands.data(), shortlist, &n);
+    if (st != SGE_OK) return st;
+    if (n == 0) return fail(SGE_BAD_INPUT, "sge_plan_pattern_sampled: no candidate plan");
+    sge_count_opts o{};
+    o.root_stride = std::max<uint64_t>(sample_stride, 1);
+    o.root_offset = 0;
+    o.collect_counters = 1;
+    uint32_t best = 0;
+    double best_ms = -1, best_work = -1;
+    for (uint32_t i = 0; i < n; ++i) {
+        sge_plan *p = nullptr;
+        if ((st = sge_plan_create(&cands[i], &p)) != SGE_OK) return st;
+        uint64_t cnt = 0;
+        sge_stats ss{};
+        o.time_budget_s = best_ms < 0 ? 0.5 : std::min(0.5, std::max(2e-3, 4.0 * best_ms / 1e3));
+        st = sge_count(g, &p, 1, &o, &cnt, nullptr, &ss);
+        sge_plan_destroy(p);
+        double ms = -1;
+        if (st == SGE_OK) ms = ss.kernel_ms;
+        else if (st != SGE_TIMEOUT) return st;
+        if (sampled_ms) sampled_ms[i] = ms;
+        if (ms < 0) continue;
+        const double work = (double)ss.alg_bytes + 64.0 * (double)ss.set_ops;
+        if (best_work < 0 || work < best_work) { best_work = work; best = i; }
+        if (best_ms < 0 || ms < best_ms) best_ms = ms;
+    }
+    if (sampled_ms)
+        for (uint32_t i = n; i < shortlist; ++i) sampled_ms[i] = -1;
+    *out = cands[best];
+    return SGE_OK;
 }
 
 // ---- batches replayed from a captured CUDA graph ----

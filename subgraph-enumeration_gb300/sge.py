@@ -131,6 +131,8 @@ SIGNATURES = {
     "sge_graph_get_info": (C.c_int, [C.c_void_p, _P(GraphInfo)]),
     "sge_graph_create_from_device_edges": (C.c_int, [C.c_void_p, u64, u32, C.c_int, _P(C.c_void_p)]),
     "sge_graph_create_rmat": (C.c_int, [u32, u64, u32, u32, u32, u64, C.c_int, _P(C.c_void_p)]),
+    "sge_plan_pattern_sampled": (C.c_int, [u32, u32, _P(u32), C.c_void_p, _P(PlanOpts), u32, u64, _P(PlanBlob),
+                                           _P(C.c_double)]),
     "sge_graph_copy_csr": (C.c_int, [C.c_void_p, _P(u32), _P(u32)]),
     "sge_plan_create": (C.c_int, [_P(PlanBlob), _P(C.c_void_p)]),
     "sge_plan_destroy": (C.c_int, [C.c_void_p]),
@@ -341,6 +343,22 @@ def plan(pattern: PatternGraph, graph: "Engine | GraphStats | DataGraph | None" 
         _check(lib().sge_plan_pattern(pattern.k, pattern.m, _u32p(e), graph._h if graph else None, C.byref(o),
                                       C.byref(b)))
     return b
+
+
+def plan_sampled(pattern: PatternGraph, engine: "Engine", iep: bool = True, exploration: bool = False,
+                 max_tail: int = SGE_MAX_TAIL, shortlist: int = 8, sample_stride: int = 64,
+                 seed: int = 1) -> tuple[PlanBlob, list[float]]:
+    """Plans with GPU root sampling (sge_plan_pattern_sampled): the cost
+    model's best `shortlist` candidates count the roots t ≡ 0 (mod
+    sample_stride) and the fastest wins.  Returns (plan, per-candidate
+    sample times in ms, -1 for candidates past the budget or absent)."""
+    o = PlanOpts(JOIN_EXPLORATION if exploration else JOIN_WCOJ, int(iep), max_tail, seed, None)
+    b = PlanBlob()
+    e = pattern.flat()
+    ms = (C.c_double * shortlist)()
+    _check(lib().sge_plan_pattern_sampled(pattern.k, pattern.m, _u32p(e), engine._h, C.byref(o), shortlist,
+                                          sample_stride, C.byref(b), ms))
+    return b, list(ms)
 
 
 SGE_FEATURES = 64

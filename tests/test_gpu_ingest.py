@@ -77,3 +77,4 @@ def test_empty_and_bad_edge_lists(sge):
     assert ei.value.status_name == "BAD_INPUT"
     with pytest.raises(sge.SgeError):
         sge.Engine.rmat_device(4, 1000, seed=1)  # too dense for 16 vertices
+
