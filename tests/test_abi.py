@@ -98,3 +98,31 @@ def test_pattern_orbit_spec_relabels(sge, tmp_path):
     f.write_text("4 3\n0 1\n1 2\n2 3\n7 1\n")
     with pytest.raises(sge.SgeError):
         sge.PatternGraph.load(f)
+
+
+def test_device_ingest_checks_arguments_before_touching_a_device(sge):
+    lib = sge.lib()
+    h = C.c_void_p()
+    # R-MAT: bad scale, a+b+c > 1, too dense for the vertex count
+    assert sge.STATUS[lib.sge_graph_create_rmat(0, 10, 570000, 190000, 190000, 1, 0, C.byref(h))] == "BAD_INPUT"
+    assert sge.STATUS[lib.sge_graph_create_rmat(8, 10, 600000, 300000, 200000, 1, 0, C.byref(h))] == "BAD_INPUT"
+    assert sge.STATUS[lib.sge_graph_create_rmat(4, 1000, 570000, 190000, 190000, 1, 0, C.byref(h))] == "BAD_INPUT"
+    # device edge list: null pointer with edges, more than 2^31 edges
+    assert sge.STATUS[lib.sge_graph_create_from_device_edges(None, 5, 10, 0, C.byref(h))] == "BAD_INPUT"
+    assert sge.STATUS[lib.sge_graph_create_from_device_edges(C.c_void_p(16), 1 << 31, 10, 0, C.byref(h))] == "BAD_INPUT"
+    assert sge.STATUS[lib.sge_graph_copy_csr(None, None, None)] == "BAD_INPUT"
+    # sampled planning needs a graph
+    b = sge.PlanBlob()
+    e = np.array([0, 1, 1, 2, 2, 0], np.uint32)
+    assert sge.STATUS[lib.sge_plan_pattern_sampled(3, 3, sge._u32p(e), None, None, 4, 8, C.byref(b), None)] == "BAD_INPUT"
+
+
+def test_device_ingest_without_a_device_is_an_error(sge):
+    if sge.lib().sge_device_count() > 0:
+        pytest.skip("a GPU is visible")
+    with pytest.raises(sge.SgeError) as e:
+        sge.Engine.rmat_device(10, 5000, seed=1)
+    assert e.value.status_name == "NO_DEVICE"
+    with pytest.raises(sge.SgeError) as e:
+        sge.Engine.from_device_edges(0, 0, 10)
+    assert e.value.status_name == "NO_DEVICE"
