@@ -6,19 +6,24 @@
 // subtreeSharedJoin (matching/parallel.cpp:167-1844).  The reference gives one
 // OpenMP task per root (a candidate of the first shared attribute, or a data
 // edge, parallel.cpp:1272,1414); here one warp owns one root edge at a time,
-// taken from a global atomic queue, and runs the plan's depth-first search
-// with all 32 lanes cooperating on every set operation:
+// taken from a per-plan atomic queue, and runs the plan's depth-first search:
 //   - candidate generation = bound trimming (setBeginPos/setEndPos,
 //     utility/utils.cpp:581-612) + k-way intersection (ComputeCandidates /
-//     MultiIntersection, utility/compute_set_intersection.cpp:10-87,308-342)
-//     done as a warp-parallel membership test of the shortest list against
-//     the others (binary search per lane), compacted with ballot/popc;
-//   - the last tail_len levels are counted, not enumerated: numResults
+//     MultiIntersection, utility/compute_set_intersection.cpp:10-87,308-342),
+//     done as a warp-parallel membership test of one list against the others:
+//     shared-memory bitmap/hash probes for the root's pinned lists, binary
+//     search otherwise, compacted with ballot/popc;
+//   - the last two enumerated levels run as one step flattened over
+//     (candidate, element) pairs across the lanes ("pair step");
+//   - the last tail_len levels are counted, not enumerated, 32 candidates at
+//     a time with their list scans flattened across the lanes: numResults
 //     (relation/relation.cpp:290-338), choosec (utils.cpp:80-94) and the
 //     inclusion–exclusion of numUniqueCombine (utils.cpp:290-350);
 //   - exploration style (-i) keeps running candidate lists per later level,
 //     updated as soon as a parent is matched (join.cpp:266-307).
-// Counts are exact uint64 (wrapping like the reference's size_t).
+// The DFS is latency-bound, so the per-warp state is kept small enough for 28
+// resident warps per SM.  Counts are exact uint64 (wrapping like the
+// reference's size_t).
 #include <cuda_runtime.h>
 
 #include <algorithm>
