@@ -2,7 +2,8 @@
 // plan's log runtime from its features.  It stands in for the cost the
 // reference's optimizer minimises (computeOrderCost / optCostOrder,
 // plan/optimizer.cpp:319-577, fed by cardEstimateUnlabeled,
-// plan/estimator.cpp:562-661); the cost model stays as fallback and judge.
+// plan/estimator.cpp:562-661); the cost model stays as the fallback and as
+// the baseline the scorer is compared with.
 //
 // Training runs on the GPU in FP32 with this file's kernels (tiled SGEMM,
 // bias/ReLU epilogues, column-sum bias gradients, Adam).  Batched inference

@@ -103,8 +103,8 @@ __global__ void scan_single_block(uint32_t *a, unsigned long long m) {
     }
 }
 
-// stable scatter: rank = tile offset of the digit + earlier rounds of this tile
-// + earlier warps of this round + earlier lanes with the same digit
+// stable scatter: rank = tile offset of the digit + earlier passes over this
+// tile + earlier warps of this pass + earlier lanes with the same digit
 __global__ void scatter_kernel(const uint32_t *t, const uint32_t *perm_in, uint32_t *perm_out, unsigned long long n,
                                uint32_t arity, uint32_t col, uint32_t shift, const uint32_t *offs, uint32_t ntiles) {
     __shared__ uint32_t base_off[256];
