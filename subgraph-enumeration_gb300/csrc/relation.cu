@@ -249,11 +249,13 @@ sge_status sge_sort_tuples(uint32_t *d_tuples, uint64_t n, uint32_t arity) {
     if (n <= 1) return SGE_OK;
     if (n >= (1ull << 32)) return fail(SGE_UNSUPPORTED, "sge_sort_tuples: more than 2^32 rows");
     const uint32_t ntiles = (uint32_t)((n + SORT_TILE - 1) / SORT_TILE);
-    uint32_t *pa = nullptr, *pb = nullptr, *hist = nullptr, *rows = nullptr;
-    auto cleanup = [&]() { cudaFree(pa); cudaFree(pb); cudaFree(hist); cudaFree(rows); };
+    uint32_t *pa = nullptr, *pb = nullptr, *hist = nullptr, *rows = nullptr, *sums = nullptr;
+    auto cleanup = [&]() { cudaFree(pa); cudaFree(pb); cudaFree(hist); cudaFree(rows); cudaFree(sums); };
     cudaError_t e;
+    const unsigned long long nh = 256ull * ntiles;  // digit-major histogram entries
     if ((e = cudaMalloc(&pa, n * 4)) != cudaSuccess || (e = cudaMalloc(&pb, n * 4)) != cudaSuccess ||
-        (e = cudaMalloc(&hist, (size_t)256 * ntiles * 4)) != cudaSuccess ||
+        (e = cudaMalloc(&hist, nh * 4)) != cudaSuccess ||
+        (e = cudaMalloc(&sums, ((nh + 1023) / 1024) * 4)) != cudaSuccess ||
         (e = cudaMalloc(&rows, n * arity * 4ull)) != cudaSuccess) {
         cleanup();
         return fail(SGE_OOM, "sge_sort_tuples: %s", cudaGetErrorString(e));
@@ -262,7 +264,13 @@ sge_status sge_sort_tuples(uint32_t *d_tuples, uint64_t n, uint32_t arity) {
     for (int col = (int)arity - 1; col >= 0; --col)
         for (uint32_t shift = 0; shift < 32; shift += 8) {
             hist_kernel<<<ntiles, SORT_THREADS>>>(d_tuples, pa, n, arity, (uint32_t)col, shift, hist, ntiles);
-            scan_single_block<<<1, 1024>>>(hist, 256ull * ntiles);
+            // offsets: exclusive scan of the histogram, in place (per-1024 block scans, then
+            // one block over the block sums)
+            const sge_status sst = exclusive_scan(hist, hist, nh, sums, 0);
+            if (sst != SGE_OK) {
+                cleanup();
+                return sst;
+            }
             scatter_kernel<<<ntiles, SORT_THREADS>>>(d_tuples, pa, pb, n, arity, (uint32_t)col, shift, hist, ntiles);
             std::swap(pa, pb);
         }
