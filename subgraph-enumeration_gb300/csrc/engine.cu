@@ -1071,6 +1071,7 @@ __device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32
         uint32_t blen = 0;
         int32_t bsrc = -1;
         uint32_t x = 0, xl = 0;
+        unsigned long long pbytes = 0;  // this lane's algorithmic bytes (instrumented kernel)
         const uint32_t *xp = nullptr;
         if (lane < nc) {
             x = S.x[lane];
@@ -1103,7 +1104,7 @@ __device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32
                 for (uint32_t q = 0; q < ns; ++q)
                     if ((int32_t)q != bsrc) by += 8ull + 4ull * S.slen[q];
                 if (xpar && bsrc != -1) by += 8ull + 4ull * xl;
-                c.alg_bytes += by;
+                pbytes += by;
             }
             Bounds b;
             b.lo = 0;
@@ -1140,10 +1141,11 @@ __device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32
                         --cnt;
                 }
                 S.tr[lane] = cnt;
-                if (STATS) c.alg_bytes += 4ull * (2u + D.nex) * (31u - __clz(fl + 1u));
+                if (STATS) pbytes += 4ull * (2u + D.nex) * (31u - __clz(fl + 1u));
             }
         }
         S.bp[lane] = bp;
+        if (STATS) c.alg_bytes += warp_sum_u64(pbytes);  // all lanes, after the per-candidate branch
         uint32_t incl = blen;
 #pragma unroll
         for (uint32_t o = 1; o < 32; o <<= 1) {

@@ -93,4 +93,13 @@ def test_iep_tails_are_used(sge, patterns, graphs):
         b = sge.plan(pattern_of(sge, patterns, name), st, iep=True)
         modes[name] = (b.tail_mode, b.tail_len)
     assert modes["light_query/p2"] == (sge.TAIL_CHOOSE, 2)
-    assert modes["light_query/p4"][1] >= 2
+    # multi-level tails are candidates whenever IEP is allowed, and the chosen
+    # plan is never modelled dearer than the cheapest of them
+    for name in ["light_query/p4", "7vertex/0"]:
+        cands = sge.candidates(pattern_of(sge, patterns, name), st, iep=True, cap=4096)
+        multi = [c for c in cands if c.tail_len >= 2]
+        assert multi, name
+        chosen = sge.plan(pattern_of(sge, patterns, name), st, iep=True)
+        assert chosen.est_cost <= min(c.est_cost for c in multi)
+    assert not any(c.tail_len >= 2 for c in sge.candidates(pattern_of(sge, patterns, "light_query/p4"), st,
+                                                           iep=False, cap=4096))
