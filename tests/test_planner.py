@@ -103,3 +103,18 @@ def test_iep_tails_are_used(sge, patterns, graphs):
         assert chosen.est_cost <= min(c.est_cost for c in multi)
     assert not any(c.tail_len >= 2 for c in sge.candidates(pattern_of(sge, patterns, "light_query/p4"), st,
                                                            iep=False, cap=4096))
+
+
+def test_pair_step_is_modelled(sge):
+    """The cost model knows that the executor counts a single-list tail inline
+    in the pair step: for house on the benchmark's Chung-Lu graph, IEP mode
+    still plans a one-level tail, and that plan is modelled below every
+    multi-level-tail candidate."""
+    g = sge.gen_chung_lu(7100, 100_000, 2.1, 1000, 2)
+    st = g.stats()
+    house = sge.PatternGraph.from_edges(5, [(0, 1), (0, 2), (0, 4), (1, 3), (1, 4), (2, 3)])
+    for expl in (False, True):
+        b = sge.plan(house, st, iep=True, exploration=expl)
+        assert b.tail_len == 1 and b.num_enum == 4
+        multi = [c for c in sge.candidates(house, st, iep=True, exploration=expl, cap=4096) if c.tail_len >= 2]
+        assert multi and b.est_cost < min(c.est_cost for c in multi)
