@@ -297,10 +297,12 @@ sge_status sge_graph_create_from_device_edges(const uint32_t *d_edges, uint64_t 
                                               sge_graph **out);
 /* R-MAT generated on the GPU: the graph of sge_gen_rmat's edges for the same
  * arguments (the same counter-based stream), built as a device graph without
- * a host round trip of the edges. */
+ * a host round trip of the edges.  No counterpart in the reference, whose
+ * data graphs come from files. */
 sge_status sge_graph_create_rmat(uint32_t scale, uint64_t m, uint32_t a_ppm, uint32_t b_ppm, uint32_t c_ppm,
                                  uint64_t seed, int device, sge_graph **out);
-/* Copies a graph's CSR to host arrays (num_vertices+1 offsets, num_directed_edges neighbours). */
+/* Copies a graph's CSR to host arrays (num_vertices+1 offsets, num_directed_edges neighbours);
+ * the counterpart of reading DataGraph's offsets/neighbours (relation/graph.h:113-213). */
 sge_status sge_graph_copy_csr(const sge_graph *g, uint32_t *offsets, uint32_t *nbrs);
 
 /* ---- compiled plans ---- */
