@@ -1684,43 +1684,14 @@ void to_devplan(const sge_plan_blob &b, DevPlan &d) {
     d.keep_full = 0;
     for (uint32_t i = 0; i < b.k; ++i)
         if (b.base[i] >= 0) d.keep_full |= 1u << b.base[i];
-    // hoist tail levels with >= 2 parents that are all matched before the last enumerated level
-    d.hoist_mask = 0;
-    if (b.join_style == SGE_JOIN_WCOJ && b.num_enum >= 3)
-        for (uint32_t i = b.num_enum; i < b.k; ++i) {
-            const uint32_t par = b.parents[i];
-            const uint32_t last = 31u - (uint32_t)__builtin_clz(par);
-            if (__builtin_popcount(par) >= 2 && last + 1 < b.num_enum) {
-                d.hoist_mask |= 1u << i;
-                d.hoist_at[i] = (uint8_t)(last < 1 ? 1u : last);
-            }
-        }
+    // hoisted tail lists, the pair step and its inline tail (shared with the cost model)
+    const ExecShape xs = exec_shape(b);
+    d.hoist_mask = xs.hoist_mask;
+    for (uint32_t i = 0; i < SGE_MAX_K; ++i) d.hoist_at[i] = xs.hoist_at[i];
     d.tail_par = 0;
     for (uint32_t i = b.num_enum; i < b.k; ++i) d.tail_par |= b.parents[i];
-    // the pair step needs every tail list to be independent of level ne-2's
-    // per-candidate state: no tail reuses level ne-1's stored list, none is
-    // hoisted right after level ne-2, and (exploration) no tail's running
-    // list intersects N(m[ne-2]) into earlier parents, which the DFS would
-    // compute once per candidate of level ne-2 and the pair leaf per pair
-    d.pair = 0;
-    if (b.num_enum >= 4) {
-        const uint32_t a = b.num_enum - 2;
-        bool ok = true;
-        for (uint32_t i = b.num_enum; i < b.k; ++i) {
-            if (b.join_style == SGE_JOIN_WCOJ && b.base[i] == (int)(b.num_enum - 1)) ok = false;
-            if (((d.hoist_mask >> i) & 1u) && d.hoist_at[i] == a) ok = false;
-            if (b.join_style == SGE_JOIN_EXPLORATION && ((b.parents[i] >> a) & 1u) && (b.parents[i] & ((1u << a) - 1u)))
-                ok = false;
-        }
-        d.pair = ok ? 1u : 0u;
-    }
-    // a single tail level that neither has level ne-1 as a parent nor is
-    // bounded by it is counted per pair without the leaf, when its lists
-    // reduce to one at run time (the count only drops y itself)
-    const uint32_t last = b.num_enum - 1;
-    d.pair_direct = (d.pair && b.tail_mode == SGE_TAIL_SINGLE && b.tail_len == 1 && b.num_enum < b.k &&
-                     !(((b.parents[b.num_enum] | b.lower[b.num_enum] | b.upper[b.num_enum]) >> last) & 1u))
-                        ? 1u : 0u;
+    d.pair = xs.pair ? 1u : 0u;
+    d.pair_direct = xs.pair_direct ? 1u : 0u;
     // exploration: the running list of a tail level whose parents below the
     // leaf are exactly levels 0 and 1 is final once the root is matched;
     // it is pinned in the third table

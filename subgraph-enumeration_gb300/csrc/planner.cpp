@@ -356,20 +356,10 @@ double plan_cost(const Pattern &p, const sge_plan_blob &b, const Moments &mo) {
     auto full_len = [&](uint32_t l) { return std::max(1e-3, L * std::pow(c, __builtin_popcount(b.parents[l]) - 1)); };
     auto base_len = [&](uint32_t i) { return b.base[i] >= 0 ? std::min(full_len(b.base[i]), L) : L; };
     // the executor runs the last two enumerated levels as one flattened step
-    // when no tail level needs level ne-2's per-candidate state (the pair
-    // step); its per-candidate overhead is amortised over 32 candidates
-    auto hoisted_at_last = [&](uint32_t i) {
-        const uint32_t par = b.parents[i];
-        const uint32_t last = 31u - (uint32_t)__builtin_clz(par);
-        return __builtin_popcount(par) >= 2 && last + 1 < ne && std::max(last, 1u) == ne - 2;
-    };
-    bool pair = ne >= 4;
-    for (uint32_t i = ne; i < k && pair; ++i) {
-        if (b.join_style == SGE_JOIN_WCOJ && (b.base[i] == (int)(ne - 1) || hoisted_at_last(i))) pair = false;
-        if (b.join_style == SGE_JOIN_EXPLORATION && ((b.parents[i] >> (ne - 2)) & 1u) &&
-            (b.parents[i] & ((1u << (ne - 2)) - 1u)))
-            pair = false;
-    }
+    // when it can (the pair step): its per-candidate overhead is amortised
+    // over 32 candidates
+    const ExecShape xs = exec_shape(b);
+    const bool pair = xs.pair;
     double N = mo.nnz / ((b.root_kind == SGE_ROOT_ANY) ? 1.0 : 2.0);
     double cost = N * 4.0;
     double Nat[SGE_MAX_K];
@@ -403,8 +393,7 @@ double plan_cost(const Pattern &p, const sge_plan_blob &b, const Moments &mo) {
     auto leaf_lists = [&](uint32_t i) { return hoisted(i) ? 1 : lists(i); };
     double leaf = 0;
     const uint32_t yb = 1u << (ne - 1);
-    if (pair && b.tail_mode == SGE_TAIL_SINGLE && k == ne + 1 && leaf_lists(ne) == 1 &&
-        !((b.parents[ne] | b.lower[ne] | b.upper[ne]) & yb)) {
+    if (xs.pair_direct && leaf_lists(ne) == 1) {
         // counted inline per pair: the candidate's count minus the pair's own vertex
         leaf = 1.0 + ((b.check[ne] & yb) ? 1.0 : 0.0);
     } else if (b.tail_mode != SGE_TAIL_IEP && leaf_lists(ne) == 1) {
