@@ -239,11 +239,14 @@ def cpu_sample(oracle, g, plans, stride, offset, threads):
 
 def cpu_baseline(sge, g, plans, budget_s=15.0):
     """The oracle port on all host cores over the same root sample of every
-    plan of the step (every stride-th root edge), the stride shrunk until the
-    sample takes about budget_s/3 .. budget_s seconds."""
+    pattern and mode of the step (every stride-th root edge), the stride
+    shrunk until the sample takes about budget_s/3 .. budget_s seconds.  The
+    plans are the reference arm's: the engine's, or for the IEP modes the best
+    inclusion-exclusion plan when that is faster on the host."""
     sys.path.insert(0, str(REPO / "oracle"))
     import oracle
     threads = os.cpu_count() or 1
+    plans, _ = make_reference_plans(sge, oracle, g, g.stats(), threads)
     stride = 1 << 14
     while True:
         total, dt, roots = cpu_sample(oracle, g, plans, stride, 7 % stride, threads)
@@ -253,7 +256,8 @@ def cpu_baseline(sge, g, plans, budget_s=15.0):
         stride = max(1, stride // max(2, min(16, int(budget_s / 2 / max(dt, 1e-3)))))
     return {"value": total / dt, "unit": "embeddings/s", "cores": threads, "kind": "port",
             "sample": f"root edges t = {7 % stride} mod {stride} of all {len(plans)} plans of a step ({roots} roots, "
-                      f"{dt:.1f} s); value = embeddings of the sample / its time"}
+                      f"{dt:.1f} s); value = embeddings of the sample / its time; IEP modes run the faster on the "
+                      "host of the engine's plan and the best inclusion-exclusion plan"}
 
 
 def main():

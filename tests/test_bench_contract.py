@@ -28,3 +28,15 @@ def test_profile_traffic_is_read_from_the_committed_summary():
     import bench
     t = bench.profile_traffic()
     assert t is None or t > 0
+
+
+def test_cpu_baseline_runs_on_the_host():
+    sys.path.insert(0, str(REPO))
+    sys.path.insert(0, str(REPO / "subgraph-enumeration_gb300"))
+    import bench
+    import sge
+    g = bench.build_workload(sge)
+    plans, _ = bench.make_plans(sge, g.stats())
+    cb = bench.cpu_baseline(sge, g, plans, budget_s=1.5)
+    assert cb["kind"] == "port" and cb["value"] > 0 and cb["cores"] >= 1
+    assert "inclusion-exclusion" in cb["sample"]
