@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define SGE_ABI_VERSION 1u
+#define SGE_ABI_VERSION 2u
 #define SGE_MAX_K 16u          /* pattern vertices supported by the device executor */
 #define SGE_MAX_TAIL 4u        /* levels counted (not enumerated) at the leaf */
 #define SGE_MAX_PARTITIONS 15u /* set partitions of a 4-vertex tail (Bell(4)) */
@@ -128,6 +128,15 @@ typedef struct sge_plan_blob {
     uint32_t single_bag;        /* 1 if the reference would run a one-bag plan */
     uint32_t num_restrictions;  /* symmetry-breaking restrictions installed */
     double   est_cost;          /* planner cost estimate (informational) */
+    /* CHOOSE leaves: 0 = the exact binomial C(n, r) mod 2^64; 1 = the
+     * reference's choosec (utility/utils.cpp:80-94): n(n-1)…(n-r+1) kept in
+     * uint64, which wraps once the product reaches 2^64 (from n = 65,538 at r = 4),
+     * then divided by r!.  Plans imported from the reference's own planner
+     * (sge_plan_from_order_text) use 1, so their "Number of matches" is the
+     * reference's even where it wraps.  Either way a product that reaches
+     * 2^64 sets bit 2 of sge_stats.status_flags. */
+    uint32_t choose_wrap;
+    uint32_t reserved;
 } sge_plan_blob;
 
 /* Planner options */
@@ -165,7 +174,9 @@ typedef struct sge_stats {
     uint64_t alg_bytes;         /* algorithmic bytes: 4·(|A'|+|B'|) per set operation + 8 B per offset pair */
     uint64_t partial_matches;   /* enumerated partial matches (all levels) */
     uint32_t gpu_launches;      /* kernels launched by this call */
-    uint32_t status_flags;      /* bit0 overflow, bit1 timeout */
+    uint32_t status_flags;      /* bit0 overflow, bit1 timeout, bit2 a CHOOSE leaf's falling product
+                                   n(n-1)…(n-r+1) reached 2^64 (the reference's choosec wraps there;
+                                   see sge_plan_blob.choose_wrap) */
 } sge_stats;
 
 typedef struct sge_graph_info {
@@ -279,6 +290,25 @@ sge_status sge_plan_pattern_sampled(uint32_t k, uint32_t m, const uint32_t *edge
                                     const sge_plan_opts *opts, uint32_t shortlist, uint64_t sample_stride,
                                     sge_plan_blob *out, double *sampled_ms);
 
+/* Imports the reference's own plan: `text` is the block
+ * HyperTree::writeToStream prints after optCostPlan ("num bags: N", then one
+ * comma-separated attribute order per bag, the global bag last;
+ * plan/decomposition.cpp:537-552, main.cpp:64-66), a whole reference log
+ * holding it, or an order file in buildTreesFromOrderFile's format
+ * (plan/optimizer.cpp:724-752).  Replaces the planning half of main.cpp:60-69
+ * for callers that keep the reference's planner: the global bag's order runs
+ * first, then each other bag's own attributes in its order (as the trie join
+ * of sharedJoin/globalJoin visits them), with this library's symmetry
+ * restrictions and leaf counting for that order.  "Number of matches"
+ * follows the imported plan's shape: embeddings for one bag, instances for
+ * several (relation/graph.cpp:910-1077).  The bags must cover every vertex
+ * and every edge of the pattern.  stats may be NULL; opts (may be NULL)
+ * gives the join style and whether the leaf may count several levels (-u).
+ * num_bags (may be NULL) receives the number of bags read. */
+sge_status sge_plan_from_order_text(uint32_t k, uint32_t m, const uint32_t *edges, const char *text,
+                                    const sge_graph_stats *stats, const sge_plan_opts *opts, sge_plan_blob *out,
+                                    uint32_t *num_bags);
+
 /* Check a plan blob for internal consistency (levels, masks, tail validity). */
 sge_status sge_plan_validate(const sge_plan_blob *blob);
 
@@ -384,9 +414,12 @@ sge_status sge_count_host(const uint32_t *offsets, const uint32_t *nbrs, uint32_
  *   plans:             host plan blobs (at most SGE_NOALLOC_MAX_PLANS)
  *   d_counts:          device uint64[nplans]; receives "Number of matches"
  *   stream:            a cudaStream_t (NULL = the default stream)
- * The call is synchronous on `stream` (it reads back the status).  The first
- * call on a device looks up the array's device address with that device
- * current; make that first call before any stream capture.  All calls share
+ * The call is synchronous on `stream` (it reads back the status).  Each call
+ * looks up the array's device address with the current device selected, so
+ * a context that was torn down and rebuilt (cudaDeviceReset) is picked up; a
+ * call made while `stream` is capturing reuses the address of the device's
+ * last call outside capture, so make the first call on a device before any
+ * stream capture.  All calls share
  * the one array, so calls whose launches overlap on the GPU race: serialise
  * them (one stream, or one call at a time per device).  A graph or plan batch
  * whose per-warp lists do not fit in the array is rejected with

@@ -47,6 +47,14 @@ def lib() -> C.CDLL:
         L.oracle_max_threads.restype = C.c_int
         L.oracle_list_embeddings.restype = u64
         L.oracle_list_embeddings.argtypes = [_P(u32), _P(u32), u32, u32, u32, _P(u32), _P(u32), u64]
+        L.oracle_gen_rmat.restype = C.c_int
+        L.oracle_gen_rmat.argtypes = [u32, u64, u32, u32, u32, u64, _P(_P(u32)), _P(u64)]
+        L.oracle_gen_chung_lu.restype = C.c_int
+        L.oracle_gen_chung_lu.argtypes = [u32, u64, u32, u32, u64, _P(_P(u32)), _P(u64)]
+        L.oracle_csr_from_sorted_edges.restype = None
+        L.oracle_csr_from_sorted_edges.argtypes = [_P(u32), u64, u32, _P(u32), _P(u32)]
+        L.oracle_free.restype = None
+        L.oracle_free.argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
@@ -151,3 +159,37 @@ def canonical_instances(emb: np.ndarray, perms: np.ndarray) -> np.ndarray:
             decided |= lt | gt
         best[less] = cand[less]
     return np.unique(best, axis=0)
+
+
+def _take_edges(ep, m: int) -> np.ndarray:
+    e = np.ctypeslib.as_array(ep, shape=(2 * max(m, 1),))[: 2 * m].copy()
+    lib().oracle_free(C.cast(ep, C.c_void_p))
+    return e
+
+
+def csr_from_sorted_edges(edges: np.ndarray, n: int) -> tuple[np.ndarray, np.ndarray]:
+    """Symmetric sorted CSR (offsets, neighbours) of sorted distinct u<v pairs."""
+    e = _arr(edges).reshape(-1)
+    m = e.size // 2
+    off = np.zeros(n + 1, np.uint32)
+    nb = np.zeros(max(2 * m, 1), np.uint32)
+    lib().oracle_csr_from_sorted_edges(_p(e), m, n, _p(off), _p(nb))
+    return off, nb[: 2 * m]
+
+
+def gen_rmat(scale: int, m: int, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+             seed: int = 0) -> tuple[np.ndarray, np.ndarray]:
+    """The library's seeded R-MAT graph (sge_gen_rmat), built without the library: (offsets, neighbours)."""
+    ep, mo = _P(u32)(), u64()
+    if not lib().oracle_gen_rmat(scale, m, round(a * 1e6), round(b * 1e6), round(c * 1e6), seed, C.byref(ep),
+                                 C.byref(mo)):
+        raise ValueError("oracle_gen_rmat: bad arguments")
+    return csr_from_sorted_edges(_take_edges(ep, mo.value), 1 << scale)
+
+
+def gen_chung_lu(n: int, m: int, gamma: float, max_deg: int = 0, seed: int = 0) -> tuple[np.ndarray, np.ndarray]:
+    """The library's seeded Chung-Lu graph (sge_gen_chung_lu), built without the library."""
+    ep, mo = _P(u32)(), u64()
+    if not lib().oracle_gen_chung_lu(n, m, round(gamma * 1000), max_deg, seed, C.byref(ep), C.byref(mo)):
+        raise ValueError("oracle_gen_chung_lu: bad arguments")
+    return csr_from_sorted_edges(_take_edges(ep, mo.value), n)

@@ -10,7 +10,9 @@
 # autotools builds are not run.  On an x86 host the reference's AVX2
 # intersection path is used; on any other host -D__APPLE__ selects its scalar
 # path (identical counts).
-REF    ?= /root/reference
+ifndef REF
+  $(error set REF to the reference checkout, e.g. make -f oracle/ref.mk REF=<path>)
+endif
 OUT    ?= oracle/_ref
 OBJ    ?= /tmp/sge_ref_obj
 ARCH   := $(shell uname -m)
@@ -46,6 +48,7 @@ GLPK_OBJ  := $(addprefix $(OBJ)/glpk/,$(GLPK_SRC:.c=.o))
 all: $(OUT)/graph_mining_system
 
 $(OUT)/graph_mining_system: $(CXX_OBJ) $(NAUTY_OBJ) $(GLPK_OBJ)
+	@mkdir -p $(OUT)
 	$(CXX) -fopenmp -o $@ $(CXX_OBJ) $(NAUTY_OBJ) $(GLPK_OBJ) -lm
 
 $(OBJ)/ref/%.o: $(REF)/%.cpp

@@ -17,6 +17,7 @@
  *     numUniqueCombine at the leaf), parallel over root edges with OpenMP like
  *     parSharedJoin (matching/parallel.cpp:1154-1486).
  */
+#include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -442,7 +443,8 @@ static uint64_t tail_count(const exec_ctx *c, const uint32_t *mm, uint32_t **buf
                                            : level_candidates(c, (i), mm, (out), tmp))
     if (p->tail_mode == SGE_TAIL_SINGLE || p->tail_mode == SGE_TAIL_CHOOSE) {
         uint32_t n = TAIL_CANDS(ne, bufs[0]);
-        return p->tail_mode == SGE_TAIL_SINGLE ? (uint64_t)n : oracle_binom_exact(n, (int)T);
+        if (p->tail_mode == SGE_TAIL_SINGLE) return (uint64_t)n;
+        return p->choose_wrap ? oracle_choosec_ref(n, (int)T) : oracle_binom_exact(n, (int)T);
     }
     const uint32_t *sets[SGE_MAX_TAIL];
     uint32_t lens[SGE_MAX_TAIL];
@@ -588,3 +590,217 @@ uint64_t oracle_list_embeddings(const uint32_t *off, const uint32_t *nb, uint32_
     }
     return total;
 }
+
+/* ---------------------------------------------------------------- 4 ----
+ * Seeded workloads without the library.  The library's seeded generators
+ * (subgraph-enumeration_gb300/csrc/generators.cpp: sge_gen_rmat,
+ * sge_gen_chung_lu) and its symmetric CSR build (sge_csr_from_edges) are
+ * restated here, on the same splitmix64 streams and integer decisions, so a
+ * CPU-only process (the timed CPU arm of bench.py) builds the very same data
+ * graphs while loading nothing but this file's library.  tests/ pin the two
+ * against each other. */
+
+static uint64_t o_splitmix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+typedef struct { uint64_t s; } o_rng;
+static void o_rng_init(o_rng *r, uint64_t seed) { r->s = o_splitmix64(seed ^ 0x5347454E5347454Eull); }
+static uint64_t o_rng_next(o_rng *r) {
+    r->s += 0x9E3779B97F4A7C15ull;
+    uint64_t z = r->s;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static uint64_t o_rng_below(o_rng *r, uint64_t n) { return (uint64_t)(((unsigned __int128)o_rng_next(r) * n) >> 64); }
+
+/* Set of distinct 64-bit edge keys (open addressing; ~0 marks a free slot),
+ * remembering insertion order. */
+typedef struct { uint64_t *slot, mask, *order, n; } o_keyset;
+static int o_keyset_init(o_keyset *s, uint64_t cap) {
+    uint64_t sz = 1;
+    while (sz < 2 * cap + 16) sz <<= 1;
+    s->slot = (uint64_t *)malloc(sizeof(uint64_t) * sz);
+    s->order = (uint64_t *)malloc(sizeof(uint64_t) * (cap + 1));
+    if (!s->slot || !s->order) { free(s->slot); free(s->order); return 0; }
+    memset(s->slot, 0xFF, sizeof(uint64_t) * sz);
+    s->mask = sz - 1;
+    s->n = 0;
+    return 1;
+}
+static void o_keyset_add(o_keyset *s, uint64_t key) {
+    uint64_t h = (key * 0x9E3779B97F4A7C15ull) >> 20;
+    for (;; ++h) {
+        uint64_t *p = &s->slot[h & s->mask];
+        if (*p == key) return;
+        if (*p == ~0ull) { *p = key; s->order[s->n++] = key; return; }
+    }
+}
+
+/* LSD radix sort of 64-bit keys (16-bit digits; digits that never vary are skipped). */
+static void o_sort_u64(uint64_t *a, uint64_t n) {
+    if (n < 2) return;
+    uint64_t *tmp = (uint64_t *)malloc(sizeof(uint64_t) * n);
+    uint64_t *cnt = (uint64_t *)malloc(sizeof(uint64_t) * 65536);
+    uint64_t *src = a, *dst = tmp;
+    for (int sh = 0; sh < 64; sh += 16) {
+        memset(cnt, 0, sizeof(uint64_t) * 65536);
+        for (uint64_t i = 0; i < n; ++i) cnt[(src[i] >> sh) & 0xFFFF]++;
+        if (cnt[(src[0] >> sh) & 0xFFFF] == n) continue;
+        uint64_t acc = 0;
+        for (int d = 0; d < 65536; ++d) { uint64_t c = cnt[d]; cnt[d] = acc; acc += c; }
+        for (uint64_t i = 0; i < n; ++i) dst[cnt[(src[i] >> sh) & 0xFFFF]++] = src[i];
+        uint64_t *t = src; src = dst; dst = t;
+    }
+    if (src != a) memcpy(a, src, sizeof(uint64_t) * n);
+    free(tmp);
+    free(cnt);
+}
+
+/* One R-MAT draw as generators.cpp's rmat_draw: `scale` quadrant choices,
+ * two per 64-bit word; ~0 for a self-loop, else (min << 32) | max. */
+static uint64_t o_rmat_draw(uint64_t seed, uint64_t idx, uint32_t scale, uint32_t ta, uint32_t tab, uint32_t tabc) {
+    uint32_t u = 0, v = 0;
+    uint64_t word = 0;
+    for (uint32_t bit = 0; bit < scale; ++bit) {
+        uint32_t r;
+        if ((bit & 1) == 0) {
+            word = o_splitmix64(seed * 0x100000001B3ull + idx * 64 + bit);
+            r = (uint32_t)word;
+        } else {
+            r = (uint32_t)(word >> 32);
+        }
+        uint32_t ub, vb;
+        if (r < ta) { ub = 0; vb = 0; }
+        else if (r < tab) { ub = 0; vb = 1; }
+        else if (r < tabc) { ub = 1; vb = 0; }
+        else { ub = 1; vb = 1; }
+        u = (u << 1) | ub;
+        v = (v << 1) | vb;
+    }
+    if (u == v) return ~0ull;
+    if (u > v) { uint32_t t = u; u = v; v = t; }
+    return ((uint64_t)u << 32) | v;
+}
+
+static uint32_t o_ppm_threshold(uint64_t ppm) {
+    uint64_t t = (ppm << 32) / 1000000u;
+    return t > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)t;
+}
+
+/* sge_gen_rmat: the m distinct edges whose first draw comes earliest in the
+ * draw stream (the library reaches the same set by drawing in rounds), as
+ * sorted u<v pairs.  *edges is malloc'ed (2·m_out uint32). */
+int oracle_gen_rmat(uint32_t scale, uint64_t m, uint32_t a_ppm, uint32_t b_ppm, uint32_t c_ppm, uint64_t seed,
+                    uint32_t **edges, uint64_t *m_out) {
+    if (scale < 1 || scale > 31) return 0;
+    const uint32_t ta = o_ppm_threshold(a_ppm), tab = o_ppm_threshold((uint64_t)a_ppm + b_ppm),
+                   tabc = o_ppm_threshold((uint64_t)a_ppm + b_ppm + c_ppm);
+    o_keyset s;
+    if (!o_keyset_init(&s, m)) return 0;
+    const uint64_t CH = 1u << 22;
+    uint64_t *buf = (uint64_t *)malloc(sizeof(uint64_t) * CH);
+    for (uint64_t base = 0; s.n < m && base < (1ull << 34); base += CH) {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+        for (int64_t i = 0; i < (int64_t)CH; ++i) buf[i] = o_rmat_draw(seed, base + (uint64_t)i, scale, ta, tab, tabc);
+        for (uint64_t i = 0; i < CH && s.n < m; ++i)
+            if (buf[i] != ~0ull) o_keyset_add(&s, buf[i]);
+    }
+    free(buf);
+    free(s.slot);
+    o_sort_u64(s.order, s.n);
+    uint32_t *e = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (s.n ? s.n : 1));
+    for (uint64_t i = 0; i < s.n; ++i) { e[2 * i] = (uint32_t)(s.order[i] >> 32); e[2 * i + 1] = (uint32_t)s.order[i]; }
+    free(s.order);
+    *edges = e;
+    *m_out = s.n;
+    return 1;
+}
+
+/* sge_gen_chung_lu: integer-rounded weights ∝ (i+1)^(-1/(gamma-1)) scaled to
+ * mean degree 2m/n and capped at max_deg; draws until m distinct edges. */
+int oracle_gen_chung_lu(uint32_t n, uint64_t m, uint32_t gamma_milli, uint32_t max_deg, uint64_t seed,
+                        uint32_t **edges, uint64_t *m_out) {
+    if (n < 2 || gamma_milli <= 1000) return 0;
+    const double alpha = 1000.0 / ((double)gamma_milli - 1000.0);
+    double *w = (double *)malloc(sizeof(double) * n);
+    double sum = 0;
+    for (uint32_t i = 0; i < n; ++i) { w[i] = pow((double)(i + 1), -alpha); sum += w[i]; }
+    const double target = 2.0 * (double)m;
+    const double cap = max_deg ? (double)max_deg : (double)(n - 1);
+    double scale = target / sum;
+    for (int it = 0; it < 8; ++it) {
+        double capped = 0, free_sum = 0;
+        for (uint32_t i = 0; i < n; ++i) {
+            double x = w[i] * scale;
+            if (x >= cap) capped += cap; else free_sum += w[i];
+        }
+        if (free_sum <= 0) break;
+        scale = (target - capped) / free_sum;
+    }
+    uint64_t *cdf = (uint64_t *)malloc(sizeof(uint64_t) * (n + 1));
+    cdf[0] = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        double x = w[i] * scale;
+        if (x > cap) x = cap;
+        uint64_t iw = (uint64_t)llround(x * 256.0);
+        if (iw == 0) iw = 1;
+        cdf[i + 1] = cdf[i] + iw;
+    }
+    free(w);
+    const uint64_t total = cdf[n];
+    o_rng rng;
+    o_rng_init(&rng, seed);
+    o_keyset s;
+    if (!o_keyset_init(&s, m)) { free(cdf); return 0; }
+    uint64_t guard = 0;
+    while (s.n < m) {
+        if (++guard > 200 * m + 100000) { free(cdf); free(s.slot); free(s.order); return 0; }
+        uint32_t uv[2];
+        for (int q = 0; q < 2; ++q) {
+            uint64_t r = o_rng_below(&rng, total);
+            uint32_t lo = 0, hi = n + 1;  /* upper_bound over cdf[0..n] */
+            while (lo < hi) { uint32_t mid = lo + (hi - lo) / 2; if (cdf[mid] <= r) lo = mid + 1; else hi = mid; }
+            uv[q] = lo - 1;
+        }
+        uint32_t u = uv[0], v = uv[1];
+        if (u == v) continue;
+        if (u > v) { uint32_t t = u; u = v; v = t; }
+        o_keyset_add(&s, ((uint64_t)u << 32) | v);
+    }
+    free(cdf);
+    free(s.slot);
+    o_sort_u64(s.order, s.n);
+    uint32_t *e = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (s.n ? s.n : 1));
+    for (uint64_t i = 0; i < s.n; ++i) { e[2 * i] = (uint32_t)(s.order[i] >> 32); e[2 * i + 1] = (uint32_t)s.order[i]; }
+    free(s.order);
+    *edges = e;
+    *m_out = s.n;
+    return 1;
+}
+
+/* Symmetric CSR of m sorted, distinct u<v edges (relation/graph.cpp:143-173,
+ * Graph::addDirectedEdges).  In (u, v) order, every vertex receives its
+ * smaller neighbours before its larger ones, each in increasing order, so the
+ * lists come out sorted.  off: n+1, nb: 2m (caller-allocated). */
+void oracle_csr_from_sorted_edges(const uint32_t *edges, uint64_t m, uint32_t n, uint32_t *off, uint32_t *nb) {
+    memset(off, 0, sizeof(uint32_t) * ((size_t)n + 1));
+    for (uint64_t i = 0; i < m; ++i) { off[edges[2 * i] + 1]++; off[edges[2 * i + 1] + 1]++; }
+    for (uint32_t v = 0; v < n; ++v) off[v + 1] += off[v];
+    uint32_t *pos = (uint32_t *)malloc(sizeof(uint32_t) * ((size_t)n + 1));
+    memcpy(pos, off, sizeof(uint32_t) * ((size_t)n + 1));
+    for (uint64_t i = 0; i < m; ++i) {
+        const uint32_t u = edges[2 * i], v = edges[2 * i + 1];
+        nb[pos[u]++] = v;
+        nb[pos[v]++] = u;
+    }
+    free(pos);
+}
+
+void oracle_free(void *p) { free(p); }

@@ -6,6 +6,24 @@
 
 namespace sge {
 
+// Restores the caller's current device when an entry point returns, so that
+// a call which selects the graph's (or scorer's) device does not move a
+// multi-GPU caller's later allocations and launches to that device.
+struct DeviceGuard {
+    int prev = -1;
+    DeviceGuard() {
+        if (cudaGetDevice(&prev) != cudaSuccess) {
+            prev = -1;
+            cudaGetLastError();
+        }
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+    DeviceGuard(const DeviceGuard &) = delete;
+    DeviceGuard &operator=(const DeviceGuard &) = delete;
+};
+
 // Exclusive prefix sum of n uint32 values in device memory (out may alias
 // nothing in `in`), ordered on stream s; temporary space is allocated here.
 sge_status device_exclusive_scan(const uint32_t *in, uint32_t *out, uint64_t n, cudaStream_t s);

@@ -85,6 +85,7 @@ struct DevPlan {
     uint32_t pair_direct;                         // pair step may count a single-list tail per pair inline
     uint32_t epin;                                // exploration: tail level whose root-level running list is pinned
     uint32_t tail_par;                            // union of the tail levels' parents
+    uint32_t choose_wrap;                         // CHOOSE leaves use the reference's wrapping choosec
 };
 static_assert(sizeof(DevPlan) % 4 == 0, "DevPlan is copied as 32-bit words");
 
@@ -93,7 +94,8 @@ struct DevStats {
 };
 
 // Flags written by kernels (never trapped on): bit0 overflow, bit1 timeout.
-enum { FLAG_OVERFLOW = 1u, FLAG_TIMEOUT = 2u };
+// bit2: a CHOOSE leaf's falling product reached 2^64 (informational).
+enum { FLAG_OVERFLOW = 1u, FLAG_TIMEOUT = 2u, FLAG_CHOOSE_WRAP = 4u };
 
 // Per-warp DFS state (shared memory).
 struct WarpState {
@@ -196,6 +198,26 @@ __device__ __forceinline__ unsigned long long binom_exact(unsigned long long n, 
     unsigned __int128 acc = 1;
     for (uint32_t i = 0; i < r; ++i) acc = acc * (unsigned __int128)(n - i) / (unsigned __int128)(i + 1);
     return (unsigned long long)acc;
+}
+
+// CHOOSE leaf: C(n, r) for the r symmetric last levels (symmLastLevel,
+// matching/join.cpp:1534-1538).  The reference's choosec
+// (utility/utils.cpp:80-94) multiplies n(n-1)…(n-r+1) in uint64 before
+// dividing by r!, so it wraps once that product reaches 2^64; wrap selects
+// its arithmetic, otherwise the exact binomial.  A product past 2^64 is
+// reported through the flags either way.
+__device__ __forceinline__ unsigned long long choose_leaf(unsigned long long n, uint32_t r, uint32_t wrap,
+                                                          uint32_t *flags) {
+    if (n < r) return 0ull;
+    unsigned long long nom = n, denom = 1;
+    unsigned __int128 wide = n;
+    for (uint32_t i = 1; i < r; ++i) {
+        nom *= n - i;
+        denom *= i + 1;
+        wide *= (unsigned __int128)(n - i);
+    }
+    if ((unsigned long long)(wide >> 64)) atomicOr(flags, FLAG_CHOOSE_WRAP);
+    return wrap ? nom / denom : binom_exact(n, r);
 }
 
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
@@ -859,7 +881,11 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
             if (a1) atomicAdd(&c.cnt[al * c.cs + i1], a1);
             a0 = a1 = 0;
         };
-        for (uint32_t j = lane; j < total; j += 32) {
+        // (a warp-uniform loop, so the periodic time check's shuffle is converged)
+        for (uint32_t j0 = 0; j0 < total; j0 += 32) {
+            if (j0 && (j0 & 0x3FFFu) == 0 && out_of_time(c)) break;
+            const uint32_t j = j0 + lane;
+            if (j >= total) break;
             while (L.pref[l] <= j) ++l;
             const uint32_t start = l ? L.pref[l - 1] : 0u;
             const uint32_t y = L.bptr[l][j - start];
@@ -898,7 +924,7 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
         r = single;
     } else if (lane < ncand) {
         if (P.tail_mode == SGE_TAIL_CHOOSE) {
-            r = binom_exact(c.cnt[(lane) * c.cs + (1)], T);
+            r = choose_leaf(c.cnt[(lane) * c.cs + (1)], T, P.choose_wrap, c.flags);
         } else {
             for (uint32_t p = 0; p < P.nparts; ++p) {
                 unsigned long long term = (unsigned long long)(long long)P.part_coef[p];
@@ -1052,7 +1078,7 @@ __device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32
     uint32_t qn = 0;
     unsigned long long isum = 0;
     bool ok = true;
-    for (uint32_t b0 = W.pos[a]; b0 < n; b0 += 32) {
+    for (uint32_t b0 = W.pos[a]; b0 < n && ok; b0 += 32) {
         if (out_of_time(c)) { ok = false; break; }
         // 1. this batch's level-a candidates, compacted
         const uint32_t idx = b0 + lane;
@@ -1158,6 +1184,7 @@ __device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32
         // 3. flattened scan; survivors are appended to the pair queue
         uint32_t l = 0;
         for (uint32_t j0 = 0; j0 < total; j0 += 32) {
+            if (j0 && (j0 & 0x1FFFu) == 0 && out_of_time(c)) { ok = false; break; }
             const uint32_t j = j0 + lane;
             bool keep = j < total;
             uint32_t y = 0;
@@ -1702,6 +1729,7 @@ void to_devplan(const sge_plan_blob &b, DevPlan &d) {
             if ((b.parents[i] & ((1u << lt) - 1u)) == 3u) d.epin = i;
     }
     d.mult = b.count_multiplier;
+    d.choose_wrap = b.choose_wrap ? 1u : 0u;
     d.chunk = 1;
     d.split_par = b.num_enum >= 3 ? (b.parents[2] & 3u) : 0u;
     for (uint32_t i = 0; i < SGE_MAX_K; ++i) d.order_[i] = (uint8_t)b.order[i];
@@ -1985,6 +2013,7 @@ sge_status sge_graph_create(const uint32_t *offsets, const uint32_t *nbrs, uint3
     int ndev = sge_device_count();
     if (ndev == 0) return fail(SGE_NO_DEVICE, "no CUDA device visible");
     if (device < 0 || device >= ndev) return fail(SGE_BAD_INPUT, "device %d out of range (%d visible)", device, ndev);
+    DeviceGuard restore_device;
     CUDA_TRY(cudaSetDevice(device));
     sge_graph *g = new sge_graph();
     g->device = device;
@@ -2092,6 +2121,7 @@ extern "C" {
 
 sge_status sge_graph_copy_csr(const sge_graph *g, uint32_t *offsets, uint32_t *nbrs) {
     if (!g || !offsets || (!nbrs && g->nnz)) return fail(SGE_BAD_INPUT, "sge_graph_copy_csr: null argument");
+    DeviceGuard restore_device;
     CUDA_TRY(cudaSetDevice(g->device));
     CUDA_TRY(cudaMemcpy(offsets, g->d_off, 4 * ((size_t)g->n + 1), cudaMemcpyDeviceToHost));
     if (g->nnz) CUDA_TRY(cudaMemcpy(nbrs, g->d_adj, 4 * g->nnz, cudaMemcpyDeviceToHost));
@@ -2100,6 +2130,7 @@ sge_status sge_graph_copy_csr(const sge_graph *g, uint32_t *offsets, uint32_t *n
 
 sge_status sge_graph_destroy(sge_graph *g) {
     if (!g) return SGE_OK;
+    DeviceGuard restore_device;
     cudaSetDevice(g->device);
     if (g->stream) cudaStreamSynchronize(g->stream);
     cudaFree(g->d_off);
@@ -2146,6 +2177,7 @@ sge_status sge_count(sge_graph *g, const sge_plan *const *plans, uint32_t nplans
     if (nplans == 0) return SGE_OK;
     sge_count_opts o{};
     if (opts) o = *opts;
+    DeviceGuard restore_device;
     CUDA_TRY(cudaSetDevice(g->device));
     LaunchCfg L;
     sge_status st = prepare_launch(g, plans, nplans, o, g->scratch_bytes, L);
@@ -2234,6 +2266,7 @@ struct sge_batch {
 
 sge_status sge_batch_destroy(sge_batch *b) {
     if (!b) return SGE_OK;
+    DeviceGuard restore_device;
     cudaSetDevice(b->g->device);
     cudaStreamSynchronize(b->g->stream);
     if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -2250,6 +2283,7 @@ sge_status sge_batch_destroy(sge_batch *b) {
 sge_status sge_batch_create(sge_graph *g, const sge_plan *const *plans, uint32_t nplans, const sge_count_opts *opts,
                             sge_batch **out) {
     if (!g || !plans || nplans == 0 || !out) return fail(SGE_BAD_INPUT, "sge_batch_create: bad argument");
+    DeviceGuard restore_device;
     CUDA_TRY(cudaSetDevice(g->device));
     sge_batch *b = new sge_batch();
     b->g = g;
@@ -2289,6 +2323,7 @@ sge_status sge_batch_run(sge_batch *b, uint64_t *counts, uint64_t *instances, sg
     auto t_start = std::chrono::steady_clock::now();
     if (!b || !counts) return fail(SGE_BAD_INPUT, "sge_batch_run: null argument");
     sge_graph *g = b->g;
+    DeviceGuard restore_device;
     CUDA_TRY(cudaSetDevice(g->device));
     CUDA_TRY(cudaEventRecord(b->ev0, g->stream));
     CUDA_TRY(cudaGraphLaunch(b->exec, g->stream));
@@ -2309,6 +2344,7 @@ sge_status sge_enumerate(sge_graph *g, const sge_plan *p, uint32_t *d_out, uint6
     if (!g || !p || !n_matches || (!d_out && capacity)) return fail(SGE_BAD_INPUT, "sge_enumerate: null argument");
     if (p->blob.tail_len != 1)
         return fail(SGE_BAD_INPUT, "sge_enumerate needs a plan with a one-level tail (plan it without IEP)");
+    DeviceGuard restore_device;
     CUDA_TRY(cudaSetDevice(g->device));
     DevPlan d = p->dp;
     d.ne = d.k;  // every level is enumerated
@@ -2457,34 +2493,46 @@ extern "C" sge_status sge_count_noalloc(const uint32_t *d_offsets, const uint32_
     int dev = 0;
     CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return fail(SGE_UNSUPPORTED, "device %d beyond the set-up table", dev);
+    // The array's device address: looked up again on every call made outside
+    // stream capture (a context torn down and rebuilt, e.g. after
+    // cudaDeviceReset, reloads the module and may move the array); a call
+    // made while `stream` is capturing uses the address of this device's last
+    // uncaptured call, so one such call must come first.
+    cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+    CUDA_TRY(cudaStreamIsCapturing(stream, &cap_status));
     void *base = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_ptr[dev]) {
+        if (cap_status == cudaStreamCaptureStatusNone) {
             void *p = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
             if (e != cudaSuccess || !p)
                 return fail(SGE_CUDA_ERROR, "cudaGetSymbolAddress(static scratch) on device %d: %s", dev,
                             cudaGetErrorString(e));
             g_noalloc_ptr[dev] = p;
+        } else if (!g_noalloc_ptr[dev]) {
+            return fail(SGE_BAD_INPUT,
+                        "sge_count_noalloc: first call on device %d made during stream capture; make one call "
+                        "outside capture first", dev);
         }
         base = g_noalloc_ptr[dev];
     }
-    // plans: validate, convert, copy into the array's plan table
+    // plans: validate, convert, copy into the array's plan table in one copy
     uint32_t nbufs = 1;
+    std::vector<DevPlan> dps(nplans);
     for (uint32_t i = 0; i < nplans; ++i) {
         sge_status st = sge_plan_validate(&plans[i]);
         if (st != SGE_OK) return st;
-        DevPlan dp;
+        DevPlan &dp = dps[i];
         to_devplan(plans[i], dp);
         dp.task_begin = 0;
         dp.ntasks = nnz;
         dp.root_stride = 1;
         dp.root_offset = 0;
         nbufs = std::max(nbufs, dp.nbufs);
-        CUDA_TRY(cudaMemcpyAsync(static_cast<unsigned char *>(base) + NOALLOC_HDR + i * sizeof(DevPlan), &dp,
-                                 sizeof(DevPlan), cudaMemcpyHostToDevice, stream));
     }
+    CUDA_TRY(cudaMemcpyAsync(static_cast<unsigned char *>(base) + NOALLOC_HDR, dps.data(), sizeof(DevPlan) * nplans,
+                             cudaMemcpyHostToDevice, stream));
     const uint32_t cap = (std::max<uint32_t>(max_degree, 1) + 31) & ~31u;
     const size_t per_warp = (size_t)nbufs * cap * sizeof(uint32_t);
     const size_t avail = SGE_NOALLOC_SCRATCH_BYTES - NOALLOC_LISTS;

@@ -165,6 +165,7 @@ sge_status sge_graph_create_from_device_edges(const uint32_t *d_edges, uint64_t 
     int ndev = sge_device_count();
     if (ndev == 0) return fail(SGE_NO_DEVICE, "no CUDA device visible");
     if (device < 0 || device >= ndev) return fail(SGE_BAD_INPUT, "device %d out of range (%d visible)", device, ndev);
+    DeviceGuard restore_device;
     CUDA_TRY(cudaSetDevice(device));
     const unsigned long long nd = 2 * m;  // directed rows
     DevBuf rows, keep, pos, src, bad;
@@ -221,6 +222,7 @@ sge_status sge_graph_create_rmat(uint32_t scale, uint64_t m, uint32_t a_ppm, uin
     int ndev = sge_device_count();
     if (ndev == 0) return fail(SGE_NO_DEVICE, "no CUDA device visible");
     if (device < 0 || device >= ndev) return fail(SGE_BAD_INPUT, "device %d out of range (%d visible)", device, ndev);
+    DeviceGuard restore_device;
     CUDA_TRY(cudaSetDevice(device));
     auto thr = [](uint64_t ppm) { return (uint32_t)std::min<uint64_t>(0xFFFFFFFFull, (ppm << 32) / 1000000u); };
     const uint32_t ta = thr(a_ppm), tab = thr((uint64_t)a_ppm + b_ppm), tabc = thr((uint64_t)a_ppm + b_ppm + c_ppm);

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "common.hpp"
+#include "device_util.hpp"
 
 using namespace sge;
 
@@ -228,6 +229,7 @@ sge_status sge_mlp_create(uint32_t in_dim, uint32_t hidden, uint64_t seed, int d
         return fail(SGE_BAD_INPUT, "sge_mlp_create: bad dimensions");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); return fail(SGE_NO_DEVICE, "no CUDA device visible"); }
+    DeviceGuard restore_device;
     CUDA_TRY(cudaSetDevice(device));
     sge_mlp *m = new sge_mlp();
     m->device = device;
@@ -261,6 +263,7 @@ sge_status sge_mlp_create(uint32_t in_dim, uint32_t hidden, uint64_t seed, int d
 
 sge_status sge_mlp_destroy(sge_mlp *m) {
     if (!m) return SGE_OK;
+    DeviceGuard restore_device;
     cudaSetDevice(m->device);
     if (m->stream) cudaStreamSynchronize(m->stream);
     cudaFree(m->d_p);
@@ -280,6 +283,7 @@ sge_status sge_mlp_num_params(const sge_mlp *m, size_t *n) {
 
 sge_status sge_mlp_get_params(const sge_mlp *m, float *out) {
     if (!m || !out) return fail(SGE_BAD_INPUT, "null argument");
+    DeviceGuard restore_device;
     CUDA_TRY(cudaSetDevice(m->device));
     CUDA_TRY(cudaMemcpy(out, m->d_p, m->np * sizeof(float), cudaMemcpyDeviceToHost));
     return SGE_OK;
@@ -287,6 +291,7 @@ sge_status sge_mlp_get_params(const sge_mlp *m, float *out) {
 
 sge_status sge_mlp_set_params(sge_mlp *m, const float *in) {
     if (!m || !in) return fail(SGE_BAD_INPUT, "null argument");
+    DeviceGuard restore_device;
     CUDA_TRY(cudaSetDevice(m->device));
     CUDA_TRY(cudaMemcpy(m->d_p, in, m->np * sizeof(float), cudaMemcpyHostToDevice));
     m->bf16_stale = true;
@@ -298,6 +303,7 @@ sge_status sge_mlp_set_params(sge_mlp *m, const float *in) {
 sge_status sge_mlp_forward(sge_mlp *m, const float *x, uint32_t B, float *y) {
     if (!m || (!x && B) || (!y && B)) return fail(SGE_BAD_INPUT, "null argument");
     if (B == 0) return SGE_OK;
+    DeviceGuard restore_device;
     CUDA_TRY(cudaSetDevice(m->device));
     sge_status st = ensure_ws(m, B);
     if (st != SGE_OK) return st;
@@ -315,6 +321,7 @@ sge_status sge_mlp_forward(sge_mlp *m, const float *x, uint32_t B, float *y) {
 sge_status sge_mlp_forward_bf16(sge_mlp *m, const float *x, uint32_t B, float *y) {
     if (!m || (!x && B) || (!y && B)) return fail(SGE_BAD_INPUT, "null argument");
     if (B == 0) return SGE_OK;
+    DeviceGuard restore_device;
     CUDA_TRY(cudaSetDevice(m->device));
     sge_status st = ensure_ws(m, B);
     if (st != SGE_OK) return st;
@@ -388,6 +395,7 @@ static sge_status loss_grad_dev(sge_mlp *m, const float *x, const float *t, uint
 
 sge_status sge_mlp_loss_grad(sge_mlp *m, const float *x, const float *t, uint32_t B, float *loss, float *grads) {
     if (!m || !x || !t || B == 0) return fail(SGE_BAD_INPUT, "sge_mlp_loss_grad: bad argument");
+    DeviceGuard restore_device;
     CUDA_TRY(cudaSetDevice(m->device));
     return loss_grad_dev(m, x, t, B, loss, true, grads);
 }
@@ -395,6 +403,7 @@ sge_status sge_mlp_loss_grad(sge_mlp *m, const float *x, const float *t, uint32_
 sge_status sge_mlp_train(sge_mlp *m, const float *x, const float *t, uint32_t n, uint32_t epochs, uint32_t batch,
                          float lr, uint64_t seed, float *final_loss) {
     if (!m || !x || !t || n == 0 || batch == 0) return fail(SGE_BAD_INPUT, "sge_mlp_train: bad argument");
+    DeviceGuard restore_device;
     CUDA_TRY(cudaSetDevice(m->device));
     std::vector<uint32_t> idx(n);
     for (uint32_t i = 0; i < n; ++i) idx[i] = i;

@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <cstddef>
 #include <vector>
@@ -633,6 +634,7 @@ sge_status sge_plan_validate(const sge_plan_blob *b) {
     if (b->join_style > SGE_JOIN_EXPLORATION) return fail(SGE_BAD_INPUT, "bad join style");
     if (b->root_kind > 2) return fail(SGE_BAD_INPUT, "bad root kind");
     if (b->count_multiplier == 0) return fail(SGE_BAD_INPUT, "count_multiplier is 0");
+    if (b->choose_wrap > 1) return fail(SGE_BAD_INPUT, "choose_wrap must be 0 or 1");
     uint32_t seen = 0;
     for (uint32_t i = 0; i < k; ++i) {
         if (b->order[i] >= k || ((seen >> b->order[i]) & 1u)) return fail(SGE_BAD_INPUT, "order is not a permutation");
@@ -708,5 +710,122 @@ extern "C" sge_status sge_pattern_automorphisms(uint32_t k, uint32_t m, const ui
     for (size_t a = 0; a < aut.size(); ++a)
         for (uint32_t j = 0; j < k; ++j) out[a * k + j] = aut[a][j];
     *naut = (uint32_t)aut.size();
+    return SGE_OK;
+}
+
+// The reference's plan as text: the block HyperTree::writeToStream prints
+// ("num bags: N" then one comma-separated attribute order per bag, global bag
+// last; plan/decomposition.cpp:537-552, printed by main.cpp:66) or an order
+// file in buildTreesFromOrderFile's format (one order per line,
+// plan/optimizer.cpp:724-752).  Other lines of a reference log (timings,
+// counts) and symmetry-rule lines ("a < b,c,") are skipped.
+static bool parse_order_line(const char *s, const char *e, std::vector<uint32_t> &out) {
+    out.clear();
+    bool any = false;
+    uint64_t cur = 0;
+    bool in_num = false;
+    for (const char *q = s; q < e; ++q) {
+        const char ch = *q;
+        if (ch >= '0' && ch <= '9') {
+            cur = cur * 10 + (uint64_t)(ch - '0');
+            if (cur > 0xFFFFu) return false;
+            in_num = any = true;
+        } else if (ch == ',' || ch == ' ' || ch == '\t' || ch == '\r') {
+            if (in_num) { out.push_back((uint32_t)cur); cur = 0; in_num = false; }
+        } else {
+            return false;
+        }
+    }
+    if (in_num) out.push_back((uint32_t)cur);
+    return any && !out.empty();
+}
+
+extern "C" sge_status sge_plan_from_order_text(uint32_t k, uint32_t m, const uint32_t *edges, const char *text,
+                                               const sge_graph_stats *stats, const sge_plan_opts *opts,
+                                               sge_plan_blob *out, uint32_t *num_bags) {
+    if (!text || !out || !edges) return fail(SGE_BAD_INPUT, "sge_plan_from_order_text: null argument");
+    Pattern p;
+    sge_status st = make_pattern(k, m, edges, p);
+    if (st != SGE_OK) return st;
+    std::vector<std::vector<uint32_t>> bags;
+    long want = -1;  // from "num bags: N"
+    std::vector<uint32_t> row;
+    for (const char *s = text; *s;) {
+        const char *e = s;
+        while (*e && *e != '\n') ++e;
+        if (strncmp(s, "num bags:", 9) == 0) {
+            want = strtol(s + 9, nullptr, 10);
+            bags.clear();
+        } else if (parse_order_line(s, e, row)) {
+            if (want < 0 || (long)bags.size() < want) bags.push_back(row);
+        }
+        s = *e ? e + 1 : e;
+        if (want >= 0 && (long)bags.size() == want) break;
+    }
+    if (bags.empty()) return fail(SGE_BAD_INPUT, "plan text holds no bag order");
+    if (want >= 0 && (long)bags.size() != want)
+        return fail(SGE_BAD_INPUT, "plan text announces %ld bags but holds %zu orders", want, bags.size());
+    // every attribute is a pattern vertex, once per bag; the bags cover the
+    // vertices and every pattern edge lies inside some bag (a decomposition)
+    uint32_t covered = 0;
+    std::vector<uint32_t> bag_mask(bags.size(), 0);
+    for (size_t b = 0; b < bags.size(); ++b)
+        for (uint32_t u : bags[b]) {
+            if (u >= k) return fail(SGE_BAD_INPUT, "bag %zu names vertex %u of a %u-vertex pattern", b, u, k);
+            if ((bag_mask[b] >> u) & 1u) return fail(SGE_BAD_INPUT, "bag %zu names vertex %u twice", b, u);
+            bag_mask[b] |= 1u << u;
+            covered |= 1u << u;
+        }
+    if (covered != ((1u << k) - 1u)) return fail(SGE_BAD_INPUT, "the bags do not cover every pattern vertex");
+    for (uint32_t a = 0; a < k; ++a)
+        for (uint32_t c = a + 1; c < k; ++c) {
+            if (!p.edge(a, c)) continue;
+            bool in = false;
+            for (uint32_t msk : bag_mask) in |= ((msk >> a) & 1u) && ((msk >> c) & 1u);
+            if (!in) return fail(SGE_BAD_INPUT, "pattern edge (%u,%u) lies in no bag", a, c);
+        }
+    // Execution order of the reference's join: the global bag's attributes in
+    // its order (the prefix shared by the bags comes first in every order),
+    // then each other bag's own attributes in its order (matched in its trie
+    // and counted at the leaf).  The device DFS needs each vertex to have an
+    // earlier neighbour and the first two to be an edge, so a vertex that has
+    // none yet waits for the first point where it does (the sequence is
+    // otherwise kept).
+    std::vector<uint32_t> seq;
+    uint32_t in_seq = 0;
+    auto take = [&](const std::vector<uint32_t> &o) {
+        for (uint32_t u : o)
+            if (!((in_seq >> u) & 1u)) { seq.push_back(u); in_seq |= 1u << u; }
+    };
+    take(bags.back());
+    for (size_t b = 0; b + 1 < bags.size(); ++b) take(bags[b]);
+    uint32_t order[SGE_MAX_K], placed = 0;
+    std::vector<bool> used(seq.size(), false);
+    for (uint32_t i = 0; i < k; ++i) {
+        size_t pick = seq.size();
+        for (size_t j = 0; j < seq.size() && pick == seq.size(); ++j) {
+            if (used[j]) continue;
+            if (i == 0 || (p.adj[seq[j]] & placed)) pick = j;
+        }
+        if (pick == seq.size()) return fail(SGE_BAD_INPUT, "the pattern is not connected");
+        used[pick] = true;
+        order[i] = seq[pick];
+        placed |= 1u << seq[pick];
+    }
+    sge_plan_opts o{};
+    o.join_style = SGE_JOIN_WCOJ;
+    o.use_iep = 1;
+    o.max_tail = SGE_MAX_TAIL;
+    if (opts) o = *opts;
+    o.force_order = order;
+    st = sge_plan_pattern_stats(k, m, edges, stats, &o, out);
+    if (st != SGE_OK) return st;
+    // "Number of matches" follows the imported plan's shape: embeddings for a
+    // one-bag plan, instances otherwise (relation/graph.cpp:910-1077,
+    // plan/decomposition.cpp:983-986)
+    out->choose_wrap = 1u;  // the reference's choosec arithmetic
+    out->single_bag = bags.size() == 1 ? 1u : 0u;
+    out->count_multiplier = bags.size() == 1 ? out->aut_size : 1u;
+    if (num_bags) *num_bags = (uint32_t)bags.size();
     return SGE_OK;
 }

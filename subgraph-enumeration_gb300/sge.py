@@ -55,7 +55,7 @@ class PlanBlob(C.Structure):
         ("num_partitions", u32), ("part_coef", i32 * SGE_MAX_PARTITIONS),
         ("part_nblocks", u32 * SGE_MAX_PARTITIONS), ("part_block", (u32 * SGE_MAX_TAIL) * SGE_MAX_PARTITIONS),
         ("count_multiplier", u64), ("aut_size", u64), ("single_bag", u32), ("num_restrictions", u32),
-        ("est_cost", C.c_double),
+        ("est_cost", C.c_double), ("choose_wrap", u32), ("reserved", u32),
     ]
 
     def summary(self) -> dict:
@@ -124,6 +124,8 @@ SIGNATURES = {
     "sge_plan_pattern": (C.c_int, [u32, u32, _P(u32), C.c_void_p, _P(PlanOpts), _P(PlanBlob)]),
     "sge_pattern_info": (C.c_int, [u32, u32, _P(u32), _P(u64), _P(u32)]),
     "sge_plan_validate": (C.c_int, [_P(PlanBlob)]),
+    "sge_plan_from_order_text": (C.c_int, [u32, u32, _P(u32), C.c_char_p, _P(GraphStats), _P(PlanOpts),
+                                           _P(PlanBlob), _P(u32)]),
     "sge_graph_stats_compute": (C.c_int, [_P(u32), _P(u32), u32, _P(GraphStats)]),
     "sge_plan_pattern_stats": (C.c_int, [u32, u32, _P(u32), _P(GraphStats), _P(PlanOpts), _P(PlanBlob)]),
     "sge_graph_create": (C.c_int, [_P(u32), _P(u32), u32, u64, C.c_int, _P(C.c_void_p)]),
@@ -343,6 +345,26 @@ def plan(pattern: PatternGraph, graph: "Engine | GraphStats | DataGraph | None" 
         _check(lib().sge_plan_pattern(pattern.k, pattern.m, _u32p(e), graph._h if graph else None, C.byref(o),
                                       C.byref(b)))
     return b
+
+
+def plan_from_reference(pattern: PatternGraph, text: str, graph: "Engine | GraphStats | DataGraph | None" = None,
+                        iep: bool = True, exploration: bool = False) -> tuple[PlanBlob, int]:
+    """Imports the reference's own plan (sge_plan_from_order_text): the bag
+    orders HyperTree::writeToStream prints ("num bags: N" + one order per bag,
+    global bag last), a whole reference log holding them, or an order file.
+    Returns (plan, number of bags)."""
+    o = PlanOpts(JOIN_EXPLORATION if exploration else JOIN_WCOJ, int(iep), SGE_MAX_TAIL, 1, None)
+    if isinstance(graph, Engine):
+        graph = graph.graph
+    if isinstance(graph, DataGraph):
+        graph = graph.stats()
+    b = PlanBlob()
+    nb = u32()
+    e = pattern.flat()
+    _check(lib().sge_plan_from_order_text(pattern.k, pattern.m, _u32p(e), text.encode(),
+                                          C.byref(graph) if graph is not None else None, C.byref(o), C.byref(b),
+                                          C.byref(nb)))
+    return b, nb.value
 
 
 def plan_sampled(pattern: PatternGraph, engine: "Engine", iep: bool = True, exploration: bool = False,

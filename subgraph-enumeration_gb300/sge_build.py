@@ -76,13 +76,19 @@ def build_oracle() -> Path:
     so = ORACLE_OUT / "liboracle.so"
     src = ORACLE / "sge_oracle.c"
     if _stale(so, [src, INC / "sge.h"]):
-        _run(["gcc", "-O3", "-std=gnu11", "-fPIC", "-shared", "-fopenmp", str(src), "-o", str(so)])
+        _run(["gcc", "-O3", "-std=gnu11", "-fPIC", "-shared", "-fopenmp", str(src), "-o", str(so), "-lm"])
     return so
 
 
-def build_reference(ref: Path = Path("/root/reference")) -> Path | None:
+def build_reference(ref: Path | None = None) -> Path | None:
     """Compiles the reference executor from its sources into oracle/_ref (only
-    where the reference checkout exists; the result is never committed)."""
+    where a reference checkout is named, by argument or by the SGE_REFERENCE
+    environment variable; the result is never committed)."""
+    if ref is None:
+        env = os.environ.get("SGE_REFERENCE")
+        if not env:
+            return None
+        ref = Path(env)
     if not (ref / "main.cpp").exists() or shutil.which("make") is None:
         return None
     _run(["make", "-f", str(ORACLE / "ref.mk"), f"REF={ref}", f"OUT={ORACLE / '_ref'}",

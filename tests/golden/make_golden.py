@@ -1,8 +1,8 @@
 """Generates the golden fixtures under tests/golden/ from the reference.
 
-Run in a checkout where the reference sources exist (default /root/reference)
-after ``__graft_entry__.build()`` has compiled oracle/_ref/graph_mining_system
-from them.  The reference itself never runs in the tests: only its recorded
+Run with SGE_REFERENCE naming a reference checkout, after
+``__graft_entry__.build()`` (with the same variable set) has compiled
+oracle/_ref/graph_mining_system from its sources.  The reference itself never runs in the tests: only its recorded
 outputs do.
 
 Outputs (all small):
@@ -29,7 +29,9 @@ REPO = HERE.parent.parent
 sys.path.insert(0, str(REPO / "subgraph-enumeration_gb300"))
 import sge  # noqa: E402
 
-REF = Path(os.environ.get("SGE_REFERENCE", "/root/reference"))
+if not os.environ.get("SGE_REFERENCE"):
+    sys.exit("set SGE_REFERENCE to the reference checkout")
+REF = Path(os.environ["SGE_REFERENCE"])
 REF_BIN = REPO / "oracle" / "_ref" / "graph_mining_system"
 
 # Synthetic data graphs with the shapes of the reference's fixtures.
