@@ -146,6 +146,15 @@ typedef struct sge_plan_opts {
     uint32_t max_tail;          /* cap on tail_len (<= SGE_MAX_TAIL) */
     uint64_t seed;              /* seed for sampling-based cost estimates */
     const uint32_t *force_order;/* optional: a full matching order to use (k entries) */
+    /* optional: k pattern vertices; every candidate's symmetry restrictions
+     * come from the stabilizer chain of this one sequence instead of from its
+     * own order.  With root_edge fixed too, all candidates keep the same
+     * representative of each instance on the same root pattern edge, so they
+     * count the same instances on any root sample (root_stride). */
+    const uint32_t *symmetry_seq;
+    /* optional: 2 adjacent pattern vertices every candidate order starts
+     * with, in either orientation */
+    const uint32_t *root_edge;
 } sge_plan_opts;
 
 /* Execution options */
@@ -155,12 +164,15 @@ typedef struct sge_count_opts {
     uint32_t chunk;             /* root tasks per queue grab; 0 = auto */
     double   time_budget_s;     /* 0 = unlimited; otherwise kernels stop and report SGE_TIMEOUT */
     uint32_t max_level_capacity;/* 0 = graph max degree; smaller values exercise the overflow path */
-    uint64_t root_stride;       /* 0/1 = every root task; s > 1: only tasks t ≡ root_offset (mod s) */
+    uint64_t root_stride;       /* 0/1 = every root edge; s > 1: only the undirected root edges e ≡ root_offset
+                                   (mod s), in CSR order (both orientations when a plan's root is unordered) */
     uint64_t root_offset;       /* (root-range sharding across ranks, or sampled runs) */
     uint32_t collect_counters;  /* 1: run the instrumented kernel (set_ops, alg_bytes, partial matches) */
     uint32_t heavy_threshold;   /* 0 = auto; otherwise roots whose level-2 list may exceed it are split
                                    into tasks of level-2 candidates (128 at four enumerated levels, a
                                    quarter as many per extra level) run by a second launch */
+    uint32_t no_hub_bitmaps;    /* 1: probe every adjacency list by binary search, ignoring the graph's
+                                   hub bitmaps (for comparison runs); 0 = use them */
 } sge_count_opts;
 
 /* Statistics of one sge_count call (per call, summed over plans).  kernel_ms,
@@ -183,7 +195,9 @@ typedef struct sge_graph_info {
     uint32_t num_vertices;
     uint64_t num_directed_edges;  /* 2m */
     uint32_t max_degree;
-    uint64_t device_bytes;        /* HBM held by the graph handle (CSR + root edges) */
+    uint64_t device_bytes;        /* HBM held by the graph handle (CSR, root edges, hub index) */
+    uint32_t hub_count;           /* vertices with a neighbour bitmap in HBM (degree >= hub_min_degree) */
+    uint32_t hub_min_degree;      /* 0xFFFFFFFF: no hub index */
 } sge_graph_info;
 
 typedef struct sge_graph sge_graph;

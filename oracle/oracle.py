@@ -44,6 +44,8 @@ def lib() -> C.CDLL:
         L.oracle_bruteforce_embeddings.argtypes = [_P(u32), _P(u32), u32, u32, u32, _P(u32), C.c_int]
         L.oracle_count_plan.restype = u64
         L.oracle_count_plan.argtypes = [_P(u32), _P(u32), u32, C.c_void_p, C.c_int, u64, u64, _P(u64)]
+        L.oracle_count_plans.restype = None
+        L.oracle_count_plans.argtypes = [_P(u32), _P(u32), u32, C.c_void_p, u32, C.c_int, u64, u64, _P(u64), _P(u64)]
         L.oracle_max_threads.restype = C.c_int
         L.oracle_list_embeddings.restype = u64
         L.oracle_list_embeddings.argtypes = [_P(u32), _P(u32), u32, u32, u32, _P(u32), _P(u32), u64]
@@ -126,6 +128,20 @@ def count_plan(offsets, nbrs, blob, threads: int = 0, stride: int = 1, offset: i
     r = lib().oracle_count_plan(_p(off), _p(nb), off.size - 1, C.addressof(blob), threads, stride, offset,
                                 C.byref(done))
     return int(r), int(done.value)
+
+
+def count_plans(offsets, nbrs, blobs: bytes, nplans: int, threads: int = 0, stride: int = 1,
+                offset: int = 0) -> tuple[list[int], list[int]]:
+    """Runs nplans plan blobs (their raw bytes back to back) over the same root
+    sample (undirected edges e ≡ offset mod stride).  Returns (instances per
+    plan, root tasks per plan)."""
+    off, nb = _arr(offsets), _arr(nbrs)
+    buf = C.create_string_buffer(bytes(blobs), len(blobs))
+    counts = (u64 * nplans)()
+    roots = (u64 * nplans)()
+    lib().oracle_count_plans(_p(off), _p(nb), off.size - 1, C.addressof(buf), nplans, threads, stride, offset,
+                             counts, roots)
+    return [int(x) for x in counts], [int(x) for x in roots]
 
 
 def max_threads() -> int:

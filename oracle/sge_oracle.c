@@ -459,18 +459,56 @@ static uint64_t tail_count(const exec_ctx *c, const uint32_t *mm, uint32_t **buf
 /* Runs the plan over root tasks t ≡ offset (mod stride).  Returns the sum of
  * per-root counts (instances; multiply by count_multiplier for the
  * reference's number). */
-uint64_t oracle_count_plan(const uint32_t *off, const uint32_t *nb, uint32_t n, const sge_plan_blob *p, int threads,
-                           uint64_t stride, uint64_t offset, uint64_t *roots_done) {
-    exec_ctx c;
-    c.off = off; c.nb = nb; c.p = p; c.maxdeg = 0;
-    for (uint32_t v = 0; v < n; ++v) if (off[v + 1] - off[v] > c.maxdeg) c.maxdeg = off[v + 1] - off[v];
-    /* root edge list u<v */
+static uint64_t count_plan_roots(const uint32_t *off, const uint32_t *nb, uint32_t maxdeg, const uint32_t *eu,
+                                 const uint32_t *ev, uint64_t m, const sge_plan_blob *p, int threads, uint64_t stride,
+                                 uint64_t offset, uint64_t *roots_done);
+
+/* Root edges u<v in CSR order (the engine's root-task numbering). */
+static uint64_t root_edges(const uint32_t *off, const uint32_t *nb, uint32_t n, uint32_t **eu, uint32_t **ev,
+                           uint32_t *maxdeg) {
     uint64_t m = off[n] / 2, w = 0;
-    uint32_t *eu = (uint32_t *)malloc(sizeof(uint32_t) * (m + 1)), *ev = (uint32_t *)malloc(sizeof(uint32_t) * (m + 1));
+    *maxdeg = 0;
+    for (uint32_t v = 0; v < n; ++v) if (off[v + 1] - off[v] > *maxdeg) *maxdeg = off[v + 1] - off[v];
+    *eu = (uint32_t *)malloc(sizeof(uint32_t) * (m + 1));
+    *ev = (uint32_t *)malloc(sizeof(uint32_t) * (m + 1));
     for (uint32_t u = 0; u < n; ++u)
         for (uint32_t e = off[u]; e < off[u + 1]; ++e)
-            if (nb[e] > u) { eu[w] = u; ev[w] = nb[e]; ++w; }
-    const uint64_t ntasks = (p->root_kind == SGE_ROOT_ANY) ? 2 * m : m;
+            if (nb[e] > u) { (*eu)[w] = u; (*ev)[w] = nb[e]; ++w; }
+    return m;
+}
+
+uint64_t oracle_count_plan(const uint32_t *off, const uint32_t *nb, uint32_t n, const sge_plan_blob *p, int threads,
+                           uint64_t stride, uint64_t offset, uint64_t *roots_done) {
+    uint32_t *eu, *ev, maxdeg;
+    const uint64_t m = root_edges(off, nb, n, &eu, &ev, &maxdeg);
+    const uint64_t r = count_plan_roots(off, nb, maxdeg, eu, ev, m, p, threads, stride, offset, roots_done);
+    free(eu);
+    free(ev);
+    return r;
+}
+
+/* Several plans over the same root sample, the root list built once:
+ * counts[i] = instances of plan i over the sampled roots, roots[i] = the
+ * root tasks it ran. */
+void oracle_count_plans(const uint32_t *off, const uint32_t *nb, uint32_t n, const sge_plan_blob *plans,
+                        uint32_t nplans, int threads, uint64_t stride, uint64_t offset, uint64_t *counts,
+                        uint64_t *roots) {
+    uint32_t *eu, *ev, maxdeg;
+    const uint64_t m = root_edges(off, nb, n, &eu, &ev, &maxdeg);
+    for (uint32_t i = 0; i < nplans; ++i)
+        counts[i] = count_plan_roots(off, nb, maxdeg, eu, ev, m, &plans[i], threads, stride, offset, &roots[i]);
+    free(eu);
+    free(ev);
+}
+
+/* Runs plan p over the sampled undirected root edges e ≡ offset (mod stride)
+ * (both orientations when the root is unordered). */
+static uint64_t count_plan_roots(const uint32_t *off, const uint32_t *nb, uint32_t maxdeg, const uint32_t *eu,
+                                 const uint32_t *ev, uint64_t m, const sge_plan_blob *p, int threads, uint64_t stride,
+                                 uint64_t offset, uint64_t *roots_done) {
+    exec_ctx c;
+    c.off = off; c.nb = nb; c.p = p; c.maxdeg = maxdeg;
+    const int64_t nor = (p->root_kind == SGE_ROOT_ANY) ? 2 : 1;
     if (stride == 0) stride = 1;
     uint64_t total = 0, done = 0;
 #ifdef _OPENMP
@@ -494,11 +532,10 @@ uint64_t oracle_count_plan(const uint32_t *off, const uint32_t *nb, uint32_t n, 
 #ifdef _OPENMP
 #pragma omp for schedule(dynamic, 64)
 #endif
-        for (int64_t ti = (int64_t)offset; ti < (int64_t)ntasks; ti += (int64_t)stride) {
-            uint64_t t = (uint64_t)ti;
-            uint32_t a, b;
-            if (p->root_kind == SGE_ROOT_ANY) { a = eu[t >> 1]; b = ev[t >> 1]; if (t & 1) { uint32_t x = a; a = b; b = x; } }
-            else { a = eu[t]; b = ev[t]; if (p->root_kind == SGE_ROOT_DESC) { uint32_t x = a; a = b; b = x; } }
+        for (int64_t ei = (int64_t)offset; ei < (int64_t)m; ei += (int64_t)stride) {
+          for (int64_t o = 0; o < nor; ++o) {
+            uint32_t a = eu[ei], b = ev[ei];
+            if ((p->root_kind == SGE_ROOT_ANY && o == 1) || p->root_kind == SGE_ROOT_DESC) { uint32_t x = a; a = b; b = x; }
             mm[0] = a; mm[1] = b;
             ++done;
             if (ne == 2) { total += tail_count(&c, mm, bufs + SGE_MAX_K, tmp, hoist, hoist_n); continue; }
@@ -517,13 +554,12 @@ uint64_t oracle_count_plan(const uint32_t *off, const uint32_t *nb, uint32_t n, 
                 cnt[lv] = level_candidates(&c, (uint32_t)lv, mm, bufs[lv], tmp);
                 it[lv] = 0;
             }
+          }
         }
         for (uint32_t i = 0; i < SGE_MAX_K + SGE_MAX_TAIL; ++i) free(bufs[i]);
         for (uint32_t i = 0; i < SGE_MAX_K; ++i) free(hoist[i]);
         free(tmp);
     }
-    free(eu);
-    free(ev);
     if (roots_done) *roots_done = done;
     return total;
 }

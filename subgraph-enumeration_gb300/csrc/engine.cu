@@ -53,6 +53,13 @@ struct DevGraph {
     const uint2 *edges;     // m undirected edges (u<v)
     uint32_t n;
     uint64_t m;
+    // Hub index: every vertex of degree >= hub_min has a bitmap of its
+    // neighbours (hub_words words over all vertex ids) at hub_slot[v], so a
+    // membership test in its list is one load instead of a binary search
+    // (hub_min = 0xFFFFFFFF: no index).
+    const uint32_t *hub_bits;
+    const int32_t *hub_slot;
+    uint32_t hub_words, hub_min;
 };
 
 // Compact device form of sge_plan_blob (+ batch bookkeeping).
@@ -107,6 +114,7 @@ struct WarpState {
     uint32_t fcnt[SGE_MAX_K];
     const uint32_t *lptr[SGE_MAX_K];      // N(m[j]) of the matched levels
     uint32_t llen[SGE_MAX_K];
+    int32_t hs[SGE_MAX_K];                // hub bitmap slot of m[j], -1 = none
     uint32_t pmode[3];                    // pinned N(m[0]), N(m[1]), level-2 list: 0 none, 1 bitmap, 2 hash
     uint32_t hcnt[SGE_MAX_K];             // hoisted tail lists (buffer slot = level)
     uint32_t hpin;                        // tail level whose hoisted list is pinned in table 2 (0 = none)
@@ -122,6 +130,7 @@ struct TailDesc {
     uint32_t exv[SGE_MAX_K];
     uint32_t lo, hi;
     uint8_t kind[SGE_MAX_K];  // 0..2 pinned table; 3 sorted list; 4/5 CSR list of slot 0/1
+    int8_t lvl[SGE_MAX_K];    // kind 3: the matched level whose CSR list it is, -1 = a stored list
     uint8_t nsrc, nex, has_lo, has_hi, lo_slots, hi_slots, ex_slots, pad;
 };
 
@@ -142,6 +151,7 @@ struct PairState {
     const uint32_t *sptr[SGE_MAX_K];  // level a+1's lists that do not depend on x
     uint32_t slen[SGE_MAX_K];
     int32_t stab[SGE_MAX_K];          // pinned table holding the list, -1 = none
+    int32_t shub[SGE_MAX_K];          // hub bitmap slot when the list is a hub's CSR list, -1 = none
     uint32_t ns;                      // number of such lists
     uint32_t xpar;                    // 1: N(x) is also one of level a+1's lists
     uint32_t exv[SGE_MAX_K];          // matched values below a that level a+1 excludes
@@ -192,6 +202,23 @@ __device__ __forceinline__ bool contains(const uint32_t *a, uint32_t n, uint32_t
     uint32_t i = lb(a, n, x);
     return i < n && a[i] == x;
 }
+
+// y ∈ N(hub) through the hub's bitmap (read-only for the whole launch).
+__device__ __forceinline__ bool hub_has(const DevGraph &g, int32_t slot, uint32_t y) {
+    return (__ldg(g.hub_bits + (size_t)slot * g.hub_words + (y >> 5)) >> (y & 31u)) & 1u;
+}
+// Bitmap slot of v given its degree (-1 below the hub threshold).
+__device__ __forceinline__ int32_t hub_slot_of(const DevGraph &g, uint32_t v, uint32_t deg) {
+    return deg >= g.hub_min ? __ldg(g.hub_slot + v) : -1;
+}
+// y ∈ N(v) for the CSR list (p, len) of vertex v.
+__device__ __forceinline__ bool csr_has(const DevGraph &g, uint32_t v, const uint32_t *p, uint32_t len, uint32_t y) {
+    const int32_t s = hub_slot_of(g, v, len);
+    return s >= 0 ? hub_has(g, s, y) : contains(p, len, y);
+}
+// Probe cost of a sorted list of len elements searched by bisection (a table
+// or bitmap probe costs 1).
+__device__ __forceinline__ uint32_t search_cost(uint32_t len) { return 2u + (31u - __clz(len + 1u)); }
 
 __device__ __forceinline__ unsigned long long binom_exact(unsigned long long n, uint32_t r) {
     if (n < r) return 0ull;
@@ -301,13 +328,14 @@ __device__ __forceinline__ bool pin_has(const uint32_t *t, uint32_t mode, uint32
 template <bool STATS>
 __device__ __forceinline__ bool in_level_list(const WarpState &W, const Ctx<STATS> &c, uint32_t j, uint32_t y) {
     if (j < 2 && W.pmode[j]) return pin_has(c.tab + j * c.tw, W.pmode[j], c.tw, y);
+    if (W.hs[j] >= 0) return hub_has(c.g, W.hs[j], y);
     return contains(W.lptr[j], W.llen[j], y);
 }
 
 // Approximate probe cost of a shared level's list (for choosing base lists).
 __device__ __forceinline__ uint32_t probe_cost(const WarpState &W, uint32_t j, uint32_t len) {
-    if (j < 2 && W.pmode[j]) return 1u;
-    return 2u + (31u - __clz(len + 1u));
+    if ((j < 2 && W.pmode[j]) || W.hs[j] >= 0) return 1u;
+    return search_cost(len);
 }
 
 // Pins a sorted list into table ti (a bitmap over all vertices, or an
@@ -400,7 +428,7 @@ __device__ __forceinline__ void set_match(const DevGraph &g, WarpState &W, uint3
     uint32_t len;
     nbr(g, x, p, len);
     __syncwarp();
-    if (lane_id() == 0) { W.m[lv] = x; W.lptr[lv] = p; W.llen[lv] = len; }
+    if (lane_id() == 0) { W.m[lv] = x; W.lptr[lv] = p; W.llen[lv] = len; W.hs[lv] = hub_slot_of(g, x, len); }
     __syncwarp();
 }
 
@@ -702,8 +730,21 @@ __device__ __forceinline__ bool td_has(const TailDesc &D, const LeafState &L, co
                                        const Ctx<STATS> &c, uint32_t q, uint32_t l, uint32_t y) {
     const uint32_t k = D.kind[q];
     if (k < 3) return pin_has(c.tab + k * c.tw, W.pmode[k], c.tw, y);
-    if (k == 3) return contains(D.ptr[q], D.len[q], y);
-    return contains(c.g.adj + L.coff[l][k - 4], L.clen[l][k - 4], y);
+    if (k == 3) {
+        const int32_t hs = D.lvl[q] >= 0 ? W.hs[D.lvl[q]] : -1;
+        return hs >= 0 ? hub_has(c.g, hs, y) : contains(D.ptr[q], D.len[q], y);
+    }
+    return csr_has(c.g, L.cm[l][k - 4], c.g.adj + L.coff[l][k - 4], L.clen[l][k - 4], y);
+}
+
+// Cost of probing list q for candidate l (1: pinned table or hub bitmap).
+__device__ __forceinline__ uint32_t td_probe_cost(const TailDesc &D, const LeafState &L, const WarpState &W,
+                                                  const DevGraph &g, uint32_t q, uint32_t l) {
+    const uint32_t k = D.kind[q];
+    if (k < 3) return 1u;
+    if (k == 3) return (D.lvl[q] >= 0 && W.hs[D.lvl[q]] >= 0) ? 1u : search_cost(D.len[q]);
+    const uint32_t len = L.clen[l][k - 4];
+    return len >= g.hub_min ? 1u : search_cost(len);
 }
 
 __device__ __forceinline__ bool td_excluded(const TailDesc &D, const LeafState &L, uint32_t l, uint32_t y) {
@@ -735,6 +776,7 @@ __device__ void tail_desc(const DevPlan &P, const WarpState &W, const LeafState 
         if (pinned) k = (src == SRC_LEVEL2_LIST || src == SRC_HOISTED) ? 2u : (uint32_t)src;
         else if (src >= (int)lc.L0 && src < SRC_LEVEL2_LIST) k = 4u + (uint32_t)src - lc.L0;
         D.kind[n] = (uint8_t)k;
+        D.lvl[n] = (int8_t)((k == 3 && src >= 0 && src < (int)lc.L0) ? src : -1);
         D.ptr[n] = p;
         D.len[n] = len;
         ++n;
@@ -834,13 +876,12 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
         {
             unsigned long long allp = 0, best = ~0ull;
             if (lane < ncand)
-                for (uint32_t q = 0; q < D.nsrc; ++q)
-                    allp += D.kind[q] < 3 ? 1u : 2u + (31u - __clz(td_len(D, L, q, lane) + 1u));
+                for (uint32_t q = 0; q < D.nsrc; ++q) allp += td_probe_cost(D, L, W, c.g, q, lane);
             for (uint32_t q = 0; q < D.nsrc; ++q) {
                 unsigned long long cost = 0;
                 if (lane < ncand) {
                     const uint32_t len = td_len(D, L, q, lane);
-                    const unsigned long long own = D.kind[q] < 3 ? 1u : 2u + (31u - __clz(len + 1u));
+                    const unsigned long long own = td_probe_cost(D, L, W, c.g, q, lane);
                     cost = (unsigned long long)len * (allp - own + 1);
                     if (STATS) bytes += 4ull * len;
                 }
@@ -991,10 +1032,12 @@ __device__ __forceinline__ void pair_sources(const DevPlan &P, const WarpState &
             const uint32_t shared = P.parents[i] & ((1u << a) - 1u);
             if (shared) {
                 const uint32_t lastp = 31 - __clz(shared);
+                S.shub[ns] = -1;
                 if (P.slot[lastp][i] < 0 && lastp < 2 && W.pmode[lastp]) {
                     S.sptr[ns] = W.lptr[lastp]; S.slen[ns] = W.llen[lastp]; S.stab[ns] = (int32_t)lastp;
                 } else {
                     S.sptr[ns] = version_ptr(P, W, c, lastp, i); S.slen[ns] = version_len(P, W, c, lastp, i); S.stab[ns] = -1;
+                    if (P.slot[lastp][i] < 0) S.shub[ns] = W.hs[lastp];
                 }
                 ++ns;
             }
@@ -1005,6 +1048,7 @@ __device__ __forceinline__ void pair_sources(const DevPlan &P, const WarpState &
                 S.sptr[ns] = W.flist[bl];
                 S.slen[ns] = W.fcnt[bl];
                 S.stab[ns] = (bl == 2 && ((P.pin_mask >> 2) & 1u) && W.pmode[2]) ? 2 : -1;
+                S.shub[ns] = -1;
                 ++ns;
                 rem = P.rest[i];
             }
@@ -1013,6 +1057,7 @@ __device__ __forceinline__ void pair_sources(const DevPlan &P, const WarpState &
                 S.sptr[ns] = W.lptr[j];
                 S.slen[ns] = W.llen[j];
                 S.stab[ns] = (j < 2 && W.pmode[j]) ? (int32_t)j : -1;
+                S.shub[ns] = W.hs[j];
                 ++ns;
             }
             xpar = (rem >> a) & 1u;
@@ -1030,8 +1075,9 @@ __device__ __forceinline__ void pair_sources(const DevPlan &P, const WarpState &
 template <bool STATS>
 __device__ __forceinline__ bool pair_in(const WarpState &W, const Ctx<STATS> &c, const PairState &S, int q,
                                         uint32_t l, uint32_t y) {
-    if (q < 0) return contains(c.g.adj + S.xo[l], S.xl[l], y);
+    if (q < 0) return csr_has(c.g, S.x[l], c.g.adj + S.xo[l], S.xl[l], y);
     if (S.stab[q] >= 0) return pin_has(c.tab + S.stab[q] * c.tw, W.pmode[S.stab[q]], c.tw, y);
+    if (S.shub[q] >= 0) return hub_has(c.g, S.shub[q], y);
     return contains(S.sptr[q], S.slen[q], y);
 }
 
@@ -1042,8 +1088,11 @@ __device__ __forceinline__ bool pair_tail_has(const WarpState &W, const Ctx<STAT
     const TailDesc &D = S.ptd;
     const uint32_t k = D.kind[0];
     if (k < 3) return pin_has(c.tab + k * c.tw, W.pmode[k], c.tw, v);
-    if (k == 3) return contains(D.ptr[0], D.len[0], v);
-    return contains(c.g.adj + S.xo[l], S.xl[l], v);
+    if (k == 3) {
+        const int32_t hs = D.lvl[0] >= 0 ? W.hs[D.lvl[0]] : -1;
+        return hs >= 0 ? hub_has(c.g, hs, v) : contains(D.ptr[0], D.len[0], v);
+    }
+    return csr_has(c.g, S.x[l], c.g.adj + S.xo[l], S.xl[l], v);
 }
 
 // The last two enumerated levels as one step: for 32 candidates x of level
@@ -1107,12 +1156,12 @@ __device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32
         }
         {
             unsigned long long allp = 0;
-            for (uint32_t q = 0; q < ns; ++q) allp += S.stab[q] >= 0 ? 1u : 2u + (31u - __clz(S.slen[q] + 1u));
-            const unsigned long long xcost = 2u + (31u - __clz(xl + 1u));
+            for (uint32_t q = 0; q < ns; ++q) allp += (S.stab[q] >= 0 || S.shub[q] >= 0) ? 1u : search_cost(S.slen[q]);
+            const unsigned long long xcost = xl >= c.g.hub_min ? 1u : search_cost(xl);
             if (xpar) allp += xcost;
             unsigned long long best = ~0ull;
             for (uint32_t q = 0; q < ns; ++q) {
-                const unsigned long long own = S.stab[q] >= 0 ? 1u : 2u + (31u - __clz(S.slen[q] + 1u));
+                const unsigned long long own = (S.stab[q] >= 0 || S.shub[q] >= 0) ? 1u : search_cost(S.slen[q]);
                 const unsigned long long cost =
                     warp_sum_u64(lane < nc ? (unsigned long long)S.slen[q] * (allp - own + 1) : 0ull);
                 if (cost < best) { best = cost; bsrc = (int32_t)q; }
@@ -1404,15 +1453,17 @@ __host__ __device__ inline uint32_t plan_cs(const DevPlan &d) {
     return d.tail_mode == SGE_TAIL_IEP ? (1u << d.T) : (d.tail_mode == SGE_TAIL_CHOOSE ? 2u : 1u);
 }
 
-// Root task t of plan P -> directed root edge (u, v).
+// Root task t of plan P -> directed root edge (u, v).  A sample (or a
+// rank's share) is the undirected edges e ≡ root_offset (mod root_stride);
+// a plan whose root is unordered (ANY) runs both orientations of each, so
+// the sample does not depend on which end of the root a plan matches first.
 __device__ __forceinline__ uint2 root_edge(const DevGraph &g, const DevPlan &P, unsigned long long t) {
-    const unsigned long long lt = P.root_offset + t * P.root_stride;
     uint2 e;
     if (P.root_kind == SGE_ROOT_ANY) {
-        e = g.edges[lt >> 1];
-        if (lt & 1) { uint32_t tmp = e.x; e.x = e.y; e.y = tmp; }
+        e = g.edges[P.root_offset + (t >> 1) * P.root_stride];
+        if (t & 1) { uint32_t tmp = e.x; e.x = e.y; e.y = tmp; }
     } else {
-        e = g.edges[lt];
+        e = g.edges[P.root_offset + t * P.root_stride];
         if (P.root_kind == SGE_ROOT_DESC) { uint32_t tmp = e.x; e.x = e.y; e.y = tmp; }
     }
     return e;
@@ -1455,8 +1506,15 @@ __global__ void __launch_bounds__(COUNT_MAX_WARPS * 32, 7) count_kernel(DevGraph
     c.set_ops = c.alg_bytes = c.partial = 0;
     WarpState &W = setup_warp(smem_raw, wib, tw, tmode, ntd, cs, nvs, c);
     unsigned long long roots = 0;
+    // The time budget covers both launch phases: phase 0's first block
+    // records its start next to the flags, and phase 1 measures from there.
     unsigned long long tstart = 0;
-    if (lane == 0) tstart = globaltimer_ns();
+    unsigned long long *t0_slot = reinterpret_cast<unsigned long long *>(flags + 2);
+    if (lane == 0) {
+        tstart = globaltimer_ns();
+        if (phase == 0 && blockIdx.x == 0 && wib == 0) *t0_slot = tstart;
+        else if (phase == 1 && *(volatile unsigned long long *)t0_slot) tstart = *(volatile unsigned long long *)t0_slot;
+    }
     c.tstart = __shfl_sync(FULL_MASK, tstart, 0);
     c.deadline = deadline_ns;
     // Plans are taken in order; each has its own task queue and chunk size, so
@@ -1635,7 +1693,20 @@ struct sge_graph {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int num_sms = 0;
     bool launched = false;     // a counting launch has run on this graph
+    // hub index (neighbour bitmaps of the highest-degree vertices)
+    uint32_t *d_hub_bits = nullptr;
+    int32_t *d_hub_slot = nullptr;
+    uint32_t hub_words = 0, hub_min = 0xFFFFFFFFu, hub_count = 0;
+    uint64_t hub_bytes = 0;
 };
+
+namespace {
+DevGraph dev_graph(const sge_graph *g, bool hubs) {
+    DevGraph d{g->d_off, g->d_adj, g->d_edges, g->n, g->m, g->d_hub_bits, g->d_hub_slot, g->hub_words, g->hub_min};
+    if (!hubs || !g->d_hub_bits) d.hub_min = 0xFFFFFFFFu;
+    return d;
+}
+}  // namespace
 
 struct sge_plan {
     sge_plan_blob blob;
@@ -1736,6 +1807,73 @@ void to_devplan(const sge_plan_blob &b, DevPlan &d) {
     d.split_S = 0;  // set per graph in sge_count
 }
 
+// Hub index: one neighbour bitmap per vertex of degree >= hub_min, with
+// hub_min the smallest threshold (at least 16: shorter lists are searched in
+// a few steps) whose bitmaps fit in min(4 GB, 1/16 of free HBM).  HBM is
+// plentiful next to the CSR, and a membership test in a hub's list, the
+// costliest binary search of the join, becomes one load.
+__global__ void hub_bits_kernel(const uint32_t *off, const uint32_t *adj, const uint32_t *hubs, uint32_t nh,
+                                uint32_t words, uint32_t *bits) {
+    for (uint32_t h = blockIdx.x; h < nh; h += gridDim.x) {
+        const uint32_t v = hubs[h];
+        uint32_t *b = bits + (size_t)h * words;
+        for (uint32_t e = off[v] + threadIdx.x; e < off[v + 1]; e += blockDim.x) {
+            const uint32_t y = adj[e];
+            atomicOr(&b[y >> 5], 1u << (y & 31u));
+        }
+    }
+}
+
+sge_status build_hub_index(sge_graph *g, const uint32_t *off) {
+    const uint32_t n = g->n;
+    if (n == 0 || g->max_deg < 16) return SGE_OK;
+    const uint64_t words = ((uint64_t)n + 31) / 32;
+    std::vector<uint32_t> hist((size_t)g->max_deg + 1, 0);
+    for (uint32_t v = 0; v < n; ++v) hist[off[v + 1] - off[v]]++;
+    size_t free_b = 0, tot_b = 0;
+    CUDA_TRY(cudaMemGetInfo(&free_b, &tot_b));
+    const uint64_t budget = std::min<uint64_t>(4ull << 30, free_b / 16);
+    const uint64_t max_hubs = std::min<uint64_t>(budget / (4 * words), 1u << 20);
+    uint64_t above = 0;
+    uint32_t thr = g->max_deg + 1;
+    for (uint32_t d = g->max_deg; d >= 16; --d) {
+        if (above + hist[d] > max_hubs) break;
+        above += hist[d];
+        thr = d;
+    }
+    if (above == 0) return SGE_OK;
+    std::vector<int32_t> slot(n, -1);
+    std::vector<uint32_t> hubs;
+    hubs.reserve(above);
+    for (uint32_t v = 0; v < n; ++v)
+        if (off[v + 1] - off[v] >= thr) { slot[v] = (int32_t)hubs.size(); hubs.push_back(v); }
+    uint32_t *d_hubs = nullptr;
+    cudaError_t e;
+    if ((e = cudaMalloc(&g->d_hub_slot, 4ull * n)) != cudaSuccess ||
+        (e = cudaMalloc(&g->d_hub_bits, 4ull * words * hubs.size())) != cudaSuccess ||
+        (e = cudaMalloc(&d_hubs, 4ull * hubs.size())) != cudaSuccess) {
+        cudaFree(g->d_hub_slot);
+        cudaFree(g->d_hub_bits);
+        g->d_hub_slot = nullptr;
+        g->d_hub_bits = nullptr;
+        cudaGetLastError();
+        return SGE_OK;  // no index: every probe is a binary search
+    }
+    CUDA_TRY(cudaMemcpyAsync(g->d_hub_slot, slot.data(), 4ull * n, cudaMemcpyHostToDevice, g->stream));
+    CUDA_TRY(cudaMemcpyAsync(d_hubs, hubs.data(), 4ull * hubs.size(), cudaMemcpyHostToDevice, g->stream));
+    CUDA_TRY(cudaMemsetAsync(g->d_hub_bits, 0, 4ull * words * hubs.size(), g->stream));
+    hub_bits_kernel<<<(unsigned)std::min<size_t>(hubs.size(), 65535), 256, 0, g->stream>>>(
+        g->d_off, g->d_adj, d_hubs, (uint32_t)hubs.size(), (uint32_t)words, g->d_hub_bits);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(g->stream));
+    cudaFree(d_hubs);
+    g->hub_words = (uint32_t)words;
+    g->hub_min = thr;
+    g->hub_count = (uint32_t)hubs.size();
+    g->hub_bytes = 4ull * words * hubs.size() + 4ull * n;
+    return SGE_OK;
+}
+
 sge_status ensure_scratch(sge_graph *g, size_t bytes) {
     if (g->scratch_bytes >= bytes) return SGE_OK;
     if (g->d_scratch) { cudaFree(g->d_scratch); g->d_scratch = nullptr; g->scratch_bytes = 0; }
@@ -1820,7 +1958,7 @@ struct LaunchCfg {
     uint32_t nplans = 0, wpb = 8, threads = 256, tmode = 0, tw = 0, cap = 0, nbufs = 1, heavy_cap = 1;
     uint32_t ntd = 1, cs = 1, nvs = 1;  // per-warp tail descriptors, leaf counters, version slots (largest plan)
     size_t smem = 0, blocks = 1, scratch_bytes = 0;
-    bool want_stats = false, any_split = false;
+    bool want_stats = false, any_split = false, use_hubs = true;
     unsigned long long deadline = 0;
     size_t off_plans = 0, off_counts = 0, off_queue = 0, off_flags = 0, off_stats = 0, off_hcnt = 0, off_hids = 0,
            bytes_zeroed = 0, bytes = 0;
@@ -1836,13 +1974,13 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
         DevPlan &d = L.dps[i];
         d = plans[i]->dp;
         d.task_begin = total;
-        const unsigned long long all = (d.root_kind == SGE_ROOT_ANY) ? 2ull * g->m : g->m;
         const unsigned long long stride = o.root_stride > 1 ? o.root_stride : 1ull;
         const unsigned long long offs = o.root_offset;
         if (stride > 1 && offs >= stride) return fail(SGE_BAD_INPUT, "root_offset %llu >= root_stride %llu", offs, stride);
         d.root_stride = stride;
         d.root_offset = stride > 1 ? offs : 0;
-        d.ntasks = all > d.root_offset ? (all - d.root_offset + stride - 1) / stride : 0;
+        const unsigned long long nedges = g->m > d.root_offset ? (g->m - d.root_offset + stride - 1) / stride : 0;
+        d.ntasks = (d.root_kind == SGE_ROOT_ANY) ? 2ull * nedges : nedges;
         total += d.ntasks;
         L.nbufs = std::max(L.nbufs, d.nbufs);
         L.ntd = std::max(L.ntd, plan_ntd(d));
@@ -1854,6 +1992,7 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
     if (g->n <= 32768u) { L.tmode = 1; L.tw = std::max<uint32_t>(32u, ((g->n + 31u) / 32u + 31u) & ~31u); }
     else { L.tmode = 2; L.tw = 512; }
     L.want_stats = o.collect_counters != 0;
+    L.use_hubs = o.no_hub_bitmaps == 0;
     // warps per block: 4 or 2, whichever keeps more warps resident per SM
     // (shared memory per warp is several KB, so smaller blocks pack better)
     int bps = 0;
@@ -1942,7 +2081,7 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
 sge_status enqueue_launch(sge_graph *g, const LaunchCfg &L, unsigned char *B, uint32_t *scratch, cudaStream_t s,
                           uint32_t &launches) {
     CUDA_TRY(cudaMemsetAsync(B + L.off_counts, 0, L.bytes_zeroed - L.off_counts, s));
-    DevGraph dg{g->d_off, g->d_adj, g->d_edges, g->n, g->m};
+    DevGraph dg = dev_graph(g, L.use_hubs);
     const DevPlan *dplans = reinterpret_cast<const DevPlan *>(B + L.off_plans);
     unsigned long long *dcounts = reinterpret_cast<unsigned long long *>(B + L.off_counts);
     unsigned long long *dqueue = reinterpret_cast<unsigned long long *>(B + L.off_queue);
@@ -2045,6 +2184,8 @@ sge_status sge_graph_create(const uint32_t *offsets, const uint32_t *nbrs, uint3
         (g->m && (e = cudaMemcpyAsync(g->d_edges, edges.data(), sizeof(uint2) * g->m, cudaMemcpyHostToDevice, g->stream)) != cudaSuccess) ||
         (e = cudaStreamSynchronize(g->stream)) != cudaSuccess)
         return cleanup(fail(SGE_CUDA_ERROR, "graph upload failed: %s", cudaGetErrorString(e)));
+    sge_status hst = build_hub_index(g, offsets);
+    if (hst != SGE_OK) return cleanup(hst);
     *out = g;
     return SGE_OK;
 }
@@ -2113,6 +2254,8 @@ sge_status sge::graph_adopt(uint32_t *d_off, uint32_t *d_adj, uint32_t n, uint64
         return cleanup(fail(SGE_CUDA_ERROR, "graph read-back: %s", cudaGetErrorString(e)));
     for (uint32_t v = 0; v < n; ++v) g->max_deg = std::max(g->max_deg, off[v + 1] - off[v]);
     sge_graph_stats_compute(off.data(), adj.data(), n, &g->stats);
+    sge_status hst = build_hub_index(g, off.data());
+    if (hst != SGE_OK) return cleanup(hst);
     *out = g;
     return SGE_OK;
 }
@@ -2138,6 +2281,8 @@ sge_status sge_graph_destroy(sge_graph *g) {
     cudaFree(g->d_edges);
     cudaFree(g->d_scratch);
     cudaFree(g->d_batch);
+    cudaFree(g->d_hub_bits);
+    cudaFree(g->d_hub_slot);
     if (g->ev0) cudaEventDestroy(g->ev0);
     if (g->ev1) cudaEventDestroy(g->ev1);
     if (g->stream) cudaStreamDestroy(g->stream);
@@ -2150,7 +2295,9 @@ sge_status sge_graph_get_info(const sge_graph *g, sge_graph_info *info) {
     info->num_vertices = g->n;
     info->num_directed_edges = g->nnz;
     info->max_degree = g->max_deg;
-    info->device_bytes = 4ull * (g->n + 1) + 4ull * g->nnz + 8ull * g->m;
+    info->device_bytes = 4ull * (g->n + 1) + 4ull * g->nnz + 8ull * g->m + g->hub_bytes;
+    info->hub_count = g->hub_count;
+    info->hub_min_degree = g->hub_min;
     return SGE_OK;
 }
 
@@ -2376,7 +2523,7 @@ sge_status sge_enumerate(sge_graph *g, const sge_plan *p, uint32_t *d_out, uint6
     uint32_t *dflags = reinterpret_cast<uint32_t *>(dq + 2);
     CUDA_TRY(cudaMemsetAsync(dq, 0, 24, g->stream));
     CUDA_TRY(cudaMemcpyAsync(B, &d, sizeof(DevPlan), cudaMemcpyHostToDevice, g->stream));
-    DevGraph dg{g->d_off, g->d_adj, g->d_edges, g->n, g->m};
+    DevGraph dg = dev_graph(g, true);
     enum_kernel<<<(unsigned)blocks, threads, smem, g->stream>>>(dg, reinterpret_cast<const DevPlan *>(B), dq,
                                                                 g->d_scratch, cap, d.nbufs, dflags, d_out, capacity, dn);
     CUDA_TRY(cudaGetLastError());
@@ -2551,7 +2698,7 @@ extern "C" sge_status sge_count_noalloc(const uint32_t *d_offsets, const uint32_
     // clear what must start at zero: queue, flags, and the caller's counts
     CUDA_TRY(cudaMemsetAsync(base, 0, NOALLOC_HDR, stream));
     CUDA_TRY(cudaMemsetAsync(d_counts, 0, sizeof(uint64_t) * nplans, stream));
-    DevGraph dg{d_offsets, d_nbrs, nullptr, n, nnz / 2};
+    DevGraph dg{d_offsets, d_nbrs, nullptr, n, nnz / 2, nullptr, nullptr, 0u, 0xFFFFFFFFu};
     unsigned char *B = static_cast<unsigned char *>(base);
     count_kernel_noalloc<<<(unsigned)blocks, threads, smem, stream>>>(
         dg, reinterpret_cast<const DevPlan *>(B + NOALLOC_HDR), nplans, nnz,

@@ -484,12 +484,28 @@ static sge_status collect_candidates(uint32_t k, uint32_t m, const uint32_t *edg
         for (uint32_t d = 0; d < SGE_MAX_K + 2; ++d) mo.M[d] = 1e6 * std::pow(16.0, (double)d);
     }
     out.clear();
+    if (o.symmetry_seq) {
+        uint32_t seen = 0;
+        for (uint32_t i = 0; i < k; ++i) {
+            if (o.symmetry_seq[i] >= k || ((seen >> o.symmetry_seq[i]) & 1u))
+                return fail(SGE_BAD_INPUT, "symmetry_seq is not a permutation");
+            seen |= 1u << o.symmetry_seq[i];
+        }
+    }
+    if (o.root_edge && (o.root_edge[0] >= k || o.root_edge[1] >= k || !p.edge(o.root_edge[0], o.root_edge[1])))
+        return fail(SGE_BAD_INPUT, "root_edge is not an edge of the pattern");
+    std::vector<std::pair<uint32_t, uint32_t>> fixed_restr;
+    if (o.symmetry_seq) fixed_restr = restrictions(p, aut, o.symmetry_seq);
     auto consider = [&](const uint32_t *order) {
+        if (o.root_edge && !((order[0] == o.root_edge[0] && order[1] == o.root_edge[1]) ||
+                             (order[0] == o.root_edge[1] && order[1] == o.root_edge[0])))
+            return;
         // two restriction schemes: stabilize in matching order, or in reverse
-        for (int scheme = 0; scheme < 2; ++scheme) {
+        // (one, from symmetry_seq, when that is given)
+        for (int scheme = 0; scheme < (o.symmetry_seq ? 1 : 2); ++scheme) {
             uint32_t seq[SGE_MAX_K];
             for (uint32_t i = 0; i < k; ++i) seq[i] = scheme == 0 ? order[i] : order[k - 1 - i];
-            auto restr = restrictions(p, aut, seq);
+            auto restr = o.symmetry_seq ? fixed_restr : restrictions(p, aut, seq);
             uint32_t tmax = std::min<uint32_t>(o.use_iep ? o.max_tail : 1u, k - 2);
             for (uint32_t T = 1; T <= tmax; ++T) {
                 Candidate c;
@@ -507,7 +523,8 @@ static sge_status collect_candidates(uint32_t k, uint32_t m, const uint32_t *edg
             seen |= 1u << o.force_order[i];
         }
         consider(o.force_order);
-        if (out.empty()) return fail(SGE_BAD_INPUT, "force_order is not a connected order starting with an edge");
+        if (out.empty())
+            return fail(SGE_BAD_INPUT, "force_order is not a connected order starting with an edge (or the root_edge)");
     } else if (k <= 8) {
         uint32_t order[SGE_MAX_K];
         for (uint32_t i = 0; i < k; ++i) order[i] = i;

@@ -74,13 +74,13 @@ class PlanBlob(C.Structure):
 
 class PlanOpts(C.Structure):
     _fields_ = [("join_style", u32), ("use_iep", u32), ("max_tail", u32), ("seed", u64),
-                ("force_order", C.POINTER(u32))]
+                ("force_order", C.POINTER(u32)), ("symmetry_seq", C.POINTER(u32)), ("root_edge", C.POINTER(u32))]
 
 
 class CountOpts(C.Structure):
     _fields_ = [("blocks_per_sm", u32), ("warps_per_block", u32), ("chunk", u32), ("time_budget_s", C.c_double),
                 ("max_level_capacity", u32), ("root_stride", u64), ("root_offset", u64), ("collect_counters", u32),
-                ("heavy_threshold", u32)]
+                ("heavy_threshold", u32), ("no_hub_bitmaps", u32)]
 
 
 class Stats(C.Structure):
@@ -101,7 +101,8 @@ class Trie(C.Structure):
 
 
 class GraphInfo(C.Structure):
-    _fields_ = [("num_vertices", u32), ("num_directed_edges", u64), ("max_degree", u32), ("device_bytes", u64)]
+    _fields_ = [("num_vertices", u32), ("num_directed_edges", u64), ("max_degree", u32), ("device_bytes", u64),
+                ("hub_count", u32), ("hub_min_degree", u32)]
 
 
 _lib = None
@@ -325,16 +326,30 @@ def gen_chung_lu(n: int, m: int, gamma: float, max_deg: int = 0, seed: int = 0) 
 
 
 # --------------------------------------------------------------- planner ----
+def _fix(o: "PlanOpts", symmetry_seq, root_edge) -> list:
+    keep = []
+    if symmetry_seq is not None:
+        keep.append(np.ascontiguousarray(symmetry_seq, dtype=np.uint32))
+        o.symmetry_seq = _u32p(keep[-1])
+    if root_edge is not None:
+        keep.append(np.ascontiguousarray(root_edge, dtype=np.uint32))
+        o.root_edge = _u32p(keep[-1])
+    return keep
+
+
 def plan(pattern: PatternGraph, graph: "Engine | GraphStats | DataGraph | None" = None, iep: bool = True,
-         exploration: bool = False, max_tail: int = SGE_MAX_TAIL, force_order=None, seed: int = 1) -> PlanBlob:
+         exploration: bool = False, max_tail: int = SGE_MAX_TAIL, force_order=None, seed: int = 1,
+         symmetry_seq=None, root_edge=None) -> PlanBlob:
     """Plans a pattern (the host planning half of graph_mining_system).  The
     cost model reads the graph's statistics: pass the Engine, a DataGraph, or
-    precomputed GraphStats (None = a generic sparse graph)."""
+    precomputed GraphStats (None = a generic sparse graph).  symmetry_seq and
+    root_edge fix the symmetry restrictions and the root pattern edge of every
+    candidate, so plans agree on any root sample."""
     o = PlanOpts(JOIN_EXPLORATION if exploration else JOIN_WCOJ, int(iep), max_tail, seed, None)
-    keep = None
+    keep = _fix(o, symmetry_seq, root_edge)
     if force_order is not None:
-        keep = np.ascontiguousarray(force_order, dtype=np.uint32)
-        o.force_order = _u32p(keep)
+        keep.append(np.ascontiguousarray(force_order, dtype=np.uint32))
+        o.force_order = _u32p(keep[-1])
     b = PlanBlob()
     e = pattern.flat()
     if isinstance(graph, DataGraph):
@@ -391,12 +406,14 @@ def _plan_opts(iep: bool, exploration: bool, max_tail: int, seed: int) -> PlanOp
 
 
 def candidates(pattern: PatternGraph, stats: "GraphStats | None", iep: bool = True, exploration: bool = False,
-               cap: int = 64, max_tail: int = SGE_MAX_TAIL) -> list[PlanBlob]:
-    """Every executable plan of the pattern, cheapest first by the cost model."""
+               cap: int = 64, max_tail: int = SGE_MAX_TAIL, symmetry_seq=None, root_edge=None) -> list[PlanBlob]:
+    """Every executable plan of the pattern, cheapest first by the cost model
+    (symmetry_seq / root_edge as in plan())."""
     arr = (PlanBlob * cap)()
     n = u32()
     e = pattern.flat()
     o = _plan_opts(iep, exploration, max_tail, 1)
+    keep = _fix(o, symmetry_seq, root_edge)  # noqa: F841 (kept alive for the call)
     _check(lib().sge_plan_candidates(pattern.k, pattern.m, _u32p(e), C.byref(stats) if stats is not None else None,
                                      C.byref(o), arr, cap, C.byref(n)))
     return [PlanBlob.from_buffer_copy(arr[i]) for i in range(n.value)]
@@ -543,7 +560,7 @@ class Engine:
 
     def count(self, plans: list[PlanBlob], stats: bool = False, time_budget_s: float = 0.0,
               max_level_capacity: int = 0, blocks_per_sm: int = 0, warps_per_block: int = 0, chunk: int = 0,
-              root_stride: int = 1, root_offset: int = 0, heavy_threshold: int = 0):
+              root_stride: int = 1, root_offset: int = 0, heavy_threshold: int = 0, hub_bitmaps: bool = True):
         """Counts every plan over the graph in one launch.  Returns (counts,
         instances, stats-dict); counts are the reference's "Number of matches"
         (uint64).  stats=True runs the instrumented kernel (set operations,
@@ -551,7 +568,8 @@ class Engine:
         root_stride/root_offset restrict the run to root tasks
         t ≡ root_offset (mod root_stride) (sharding, sampling).  heavy_threshold
         (0 = auto) splits roots whose level-2 list may exceed it into tasks of
-        a second launch."""
+        a second launch.  hub_bitmaps=False probes every adjacency list by
+        binary search (comparison runs)."""
         handles = []
         try:
             for b in plans:
@@ -563,7 +581,7 @@ class Engine:
             inst = (u64 * len(plans))()
             st = Stats()
             o = CountOpts(blocks_per_sm, warps_per_block, chunk, time_budget_s, max_level_capacity, root_stride,
-                          root_offset, int(stats), heavy_threshold)
+                          root_offset, int(stats), heavy_threshold, int(not hub_bitmaps))
             _check(lib().sge_count(self._h, arr, len(plans), C.byref(o), counts, inst, C.byref(st)))
             return list(counts), list(inst), st.as_dict()
         finally:
@@ -617,7 +635,7 @@ class Batch:
 
     def __init__(self, engine: Engine, plans: list[PlanBlob], stats: bool = False, time_budget_s: float = 0.0,
                  blocks_per_sm: int = 0, warps_per_block: int = 0, chunk: int = 0, root_stride: int = 1,
-                 root_offset: int = 0, heavy_threshold: int = 0):
+                 root_offset: int = 0, heavy_threshold: int = 0, hub_bitmaps: bool = True):
         self.engine = engine
         self.n = len(plans)
         self._ph = []
@@ -627,7 +645,7 @@ class Batch:
             self._ph.append(ph)
         arr = (C.c_void_p * self.n)(*[h.value for h in self._ph])
         o = CountOpts(blocks_per_sm, warps_per_block, chunk, time_budget_s, 0, root_stride, root_offset, int(stats),
-                      heavy_threshold)
+                      heavy_threshold, int(not hub_bitmaps))
         h = C.c_void_p()
         try:
             _check(lib().sge_batch_create(engine._h, arr, self.n, C.byref(o), C.byref(h)))
