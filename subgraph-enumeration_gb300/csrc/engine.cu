@@ -87,7 +87,7 @@ struct DevPlan {
     uint32_t split_par;                           // level 2's parents (levels 0/1): bounds its list by degree
     uint32_t split_H;                             // roots whose level-2 bound exceeds this are deferred
     uint32_t split_S;                             // level-2 candidates per deferred task (0 = never defer)
-    uint32_t split_C;                             // deferred tasks per heavy root (max degree / S, rounded up)
+    uint32_t split_P3;                            // parts of each level-3 list per deferred task (1 = none)
     uint32_t pair;                                // 1: the last two enumerated levels run as one flattened step
     uint32_t pair_direct;                         // pair step may count a single-list tail per pair inline
     uint32_t epin;                                // exploration: tail level whose root-level running list is pinned
@@ -1305,11 +1305,13 @@ __device__ __forceinline__ bool out_of_time(Ctx<STATS> &c) {
     return true;
 }
 
-// r2b/r2e restrict the level-2 candidates processed (a heavy root is split
-// into several tasks over ranges of its level-2 list).
+// r2b/r2e restrict the level-2 candidates processed, and p3 of np3 the part
+// of each level-3 list (a heavy root is split into tasks over ranges of its
+// level-2 list and equal parts of the level-3 lists below them).
 template <bool STATS>
 __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32_t u, uint32_t v,
-                                       uint32_t r2b = 0u, uint32_t r2e = 0xFFFFFFFFu) {
+                                       uint32_t r2b = 0u, uint32_t r2e = 0xFFFFFFFFu, uint32_t p3 = 0u,
+                                       uint32_t np3 = 1u) {
     const uint32_t lane = lane_id();
     const uint32_t ne = P.ne;
     if (ne == 2) return leaf_roots(P, W, c, 1u, u, v);
@@ -1399,7 +1401,14 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
         if (explore) explore_level(P, W, c, lv);
         else if (!build_level_wcoj(P, W, c, lv)) { ok = false; break; }
         __syncwarp();
-        if (lane == 0) W.pos[lv] = 0;
+        if (lane == 0) {
+            W.pos[lv] = 0;
+            if (lv == 3 && np3 > 1) {  // this task's part of the level-3 list
+                const unsigned long long n3 = W.cnt[3];
+                W.pos[3] = (uint32_t)(n3 * p3 / np3);
+                W.cnt[3] = (uint32_t)(n3 * (p3 + 1) / np3);
+            }
+        }
         __syncwarp();
     }
     if (P.pin_mask || W.hpin) unpin_root(P, W, c);
@@ -1478,10 +1487,49 @@ __device__ __forceinline__ uint32_t level2_bound(const DevGraph &g, const DevPla
     return ub;
 }
 
+// Heavy roots deferred by phase 0: their ids, per-plan counts, and the
+// exclusive prefix of their task counts (phase 1 numbers tasks densely).
+struct HeavyBuf {
+    uint32_t *cnt;             // per plan
+    uint32_t *ids;             // plan p's list at p * cap
+    unsigned long long *pre;   // task-count prefix, parallel to ids
+    unsigned long long *tot;   // per plan: phase-1 tasks
+    uint32_t cap;
+};
+
+// A heavy root with level-2 bound b runs ceil(b / split_S) × split_P3 tasks.
+// One warp per plan scans the heavy list between the two phases.
+__global__ void heavy_prefix_kernel(DevGraph g, const DevPlan *__restrict__ plans, uint32_t nplans, HeavyBuf H) {
+    const uint32_t p = blockIdx.x, lane = threadIdx.x & 31u;
+    if (p >= nplans || threadIdx.x >= 32) return;
+    const DevPlan &P = plans[p];
+    const uint32_t n = min(H.cnt[p], H.cap);
+    unsigned long long run = 0;
+    for (uint32_t b = 0; b < n; b += 32) {
+        const uint32_t h = b + lane;
+        unsigned long long tasks = 0;
+        if (h < n && P.split_S) {
+            const uint2 e = root_edge(g, P, H.ids[(size_t)p * H.cap + h]);
+            const uint32_t b2 = level2_bound(g, P, e);
+            tasks = (unsigned long long)((b2 + P.split_S - 1) / P.split_S) * P.split_P3;
+        }
+        unsigned long long incl = tasks;
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const unsigned long long v = __shfl_up_sync(FULL_MASK, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (h < n) H.pre[(size_t)p * H.cap + h] = run + incl - tasks;
+        run += __shfl_sync(FULL_MASK, incl, 31);
+    }
+    if (lane == 0) H.tot[p] = run;
+}
+
 // Phase 0 counts every root, except that a root whose level-2 bound exceeds
 // split_H is appended to its plan's heavy list (while there is room) instead.
-// Phase 1 runs the heavy roots as split_C tasks each, task c covering level-2
-// candidates [c·S, (c+1)·S); tasks past a root's bound end at once.
+// Phase 1 runs each heavy root as ceil(bound / S) × P3 tasks: task (c, q)
+// covers level-2 candidates [c·S, (c+1)·S) and, below them, part q of P3 of
+// each level-3 list, so one root's work spreads over the whole GPU.
 // 4-warp blocks, 7 per SM: 72 registers per thread and ~8 KB of shared
 // memory per warp fit 28 resident warps (the DFS is latency-bound, so
 // resident warps set the speed)
@@ -1491,8 +1539,7 @@ __global__ void __launch_bounds__(COUNT_MAX_WARPS * 32, 7) count_kernel(DevGraph
                                                     unsigned long long *queues, unsigned long long *counts,
                                                     uint32_t *scratch, uint32_t cap, uint32_t bufs_per_warp,
                                                     uint32_t tw, uint32_t tmode, unsigned long long deadline_ns,
-                                                    uint32_t *flags, DevStats *stats, uint32_t phase,
-                                                    uint32_t *heavy_cnt, uint32_t *heavy_ids, uint32_t heavy_cap,
+                                                    uint32_t *flags, DevStats *stats, uint32_t phase, HeavyBuf H,
                                                     uint32_t ntd, uint32_t cs, uint32_t nvs) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t lane = lane_id();
@@ -1523,7 +1570,7 @@ __global__ void __launch_bounds__(COUNT_MAX_WARPS * 32, 7) count_kernel(DevGraph
     unsigned long long acc = 0, ntasks = 0;
     auto load_plan = [&](uint32_t pi) {
         const DevPlan &Q = plans[pi];
-        ntasks = phase == 0 ? Q.ntasks : (unsigned long long)min(heavy_cnt[pi], heavy_cap) * Q.split_C;
+        ntasks = phase == 0 ? Q.ntasks : H.tot[pi];
     };
     if (nplans) load_plan(0);
     while (cur < nplans) {
@@ -1542,10 +1589,20 @@ __global__ void __launch_bounds__(COUNT_MAX_WARPS * 32, 7) count_kernel(DevGraph
         }
         const unsigned long long t1 = min(t0 + chunk, ntasks);
         if (phase == 1) {
-            const uint32_t h = (uint32_t)(t0 / P.split_C), part = (uint32_t)(t0 % P.split_C);
-            const uint2 e = root_edge(g, P, heavy_ids[(size_t)cur * heavy_cap + h]);
-            if ((unsigned long long)part * P.split_S < level2_bound(g, P, e))
-                acc += run_root<STATS>(P, W, c, e.x, e.y, part * P.split_S, (part + 1) * P.split_S);
+            // the heavy root holding task t0: the last with pre[h] <= t0
+            const uint32_t hn = min(H.cnt[cur], H.cap);
+            const unsigned long long *pre = H.pre + (size_t)cur * H.cap;
+            uint32_t lo = 0, len = hn;
+            while (len > 0) {
+                const uint32_t half = len >> 1;
+                if (pre[lo + half] <= t0) { lo += half + 1; len -= half + 1; }
+                else len = half;
+            }
+            const uint32_t h = lo - 1;
+            const unsigned long long local = t0 - pre[h];
+            const uint2 e = root_edge(g, P, H.ids[(size_t)cur * H.cap + h]);
+            const uint32_t c2 = (uint32_t)(local / P.split_P3), q3 = (uint32_t)(local % P.split_P3);
+            acc += run_root<STATS>(P, W, c, e.x, e.y, c2 * P.split_S, (c2 + 1) * P.split_S, q3, P.split_P3);
             continue;
         }
         if (P.ne == 2) {
@@ -1566,10 +1623,10 @@ __global__ void __launch_bounds__(COUNT_MAX_WARPS * 32, 7) count_kernel(DevGraph
             ++roots;
             if (P.split_S && level2_bound(g, P, e) > P.split_H) {
                 uint32_t slot = 0;
-                if (lane == 0) slot = atomicAdd(heavy_cnt + cur, 1u);
+                if (lane == 0) slot = atomicAdd(H.cnt + cur, 1u);
                 slot = __shfl_sync(FULL_MASK, slot, 0);
-                if (slot < heavy_cap) {
-                    if (lane == 0) heavy_ids[(size_t)cur * heavy_cap + slot] = (uint32_t)t;
+                if (slot < H.cap) {
+                    if (lane == 0) H.ids[(size_t)cur * H.cap + slot] = (uint32_t)t;
                     continue;
                 }
             }
@@ -1960,8 +2017,8 @@ struct LaunchCfg {
     size_t smem = 0, blocks = 1, scratch_bytes = 0;
     bool want_stats = false, any_split = false, use_hubs = true;
     unsigned long long deadline = 0;
-    size_t off_plans = 0, off_counts = 0, off_queue = 0, off_flags = 0, off_stats = 0, off_hcnt = 0, off_hids = 0,
-           bytes_zeroed = 0, bytes = 0;
+    size_t off_plans = 0, off_counts = 0, off_queue = 0, off_flags = 0, off_stats = 0, off_hcnt = 0, off_htot = 0,
+           off_hids = 0, off_hpre = 0, bytes_zeroed = 0, bytes = 0;
 };
 
 sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t nplans, const sge_count_opts &o,
@@ -2046,14 +2103,19 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
         // a hub), so their tasks hold fewer candidates: 128 at four
         // enumerated levels, a quarter as many per extra level
         const uint32_t deep = d.ne > 4 ? std::min<uint32_t>(d.ne - 4, 3u) : 0u;
-        const uint32_t split_S = std::max<uint32_t>(128u >> (2 * deep), 2u);
+        // where level 3 is enumerated by the DFS (or is the pair step's
+        // level), a task takes one level-2 candidate and a part of its
+        // level-3 list: 8 parts at five enumerated levels, 16 deeper
+        const bool split3 = d.ne >= 5 || (d.ne == 4 && !d.pair);
+        const uint32_t split_P3 = split3 ? (d.ne >= 6 ? 16u : 8u) : 1u;
+        const uint32_t split_S = split3 ? 1u : std::max<uint32_t>(128u >> (2 * deep), 2u);
         const double share = (double)d.ntasks * mean_deg / (double)std::max<unsigned long long>(warps, 1);
-        const uint32_t split_H = o.heavy_threshold ? std::max(o.heavy_threshold, split_S)
-                                                   : (uint32_t)std::min(1e9, std::max(4.0 * split_S, share / 4.0));
+        const uint32_t split_H = o.heavy_threshold ? std::max(o.heavy_threshold, 4u * split_S)
+                                                   : (uint32_t)std::min(1e9, std::max(32.0, share / 4.0));
         if (d.ne >= 3 && g->max_deg > split_H) {
             d.split_S = split_S;
             d.split_H = split_H;
-            d.split_C = (g->max_deg + split_S - 1) / split_S;
+            d.split_P3 = split_P3;
             L.any_split = true;
         }
         max_tasks = std::max(max_tasks, d.ntasks);
@@ -2061,17 +2123,20 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
         else if (o.chunk) d.chunk = o.chunk;
         else d.chunk = (uint32_t)std::max<unsigned long long>(1, std::min<unsigned long long>(8, d.ntasks / (warps * 64 + 1)));
     }
-    L.heavy_cap = L.any_split ? (uint32_t)std::min<unsigned long long>(max_tasks, 1ull << 20) : 1u;
-    // buffer: plans | counts | per-plan queues | flags | stats | heavy counts | heavy lists
+    L.heavy_cap = L.any_split ? (uint32_t)std::min<unsigned long long>(max_tasks, 1ull << 18) : 1u;
+    // buffer: plans | counts | per-plan queues | flags | stats | heavy counts | heavy task totals |
+    //         heavy lists | heavy task prefixes
     L.off_plans = 0;
     L.off_counts = (sizeof(DevPlan) * nplans + 255) & ~(size_t)255;
     L.off_queue = L.off_counts + ((8 * (size_t)nplans + 255) & ~(size_t)255);
     L.off_flags = L.off_queue + ((8 * (size_t)nplans + 255) & ~(size_t)255);
     L.off_stats = L.off_flags + 256;
     L.off_hcnt = L.off_stats + 256;
-    L.off_hids = L.off_hcnt + ((4 * (size_t)nplans + 255) & ~(size_t)255);
+    L.off_htot = L.off_hcnt + ((4 * (size_t)nplans + 255) & ~(size_t)255);
+    L.off_hids = L.off_htot + ((8 * (size_t)nplans + 255) & ~(size_t)255);
     L.bytes_zeroed = L.off_hids;
-    L.bytes = L.off_hids + (((size_t)L.heavy_cap * nplans * 4 + 255) & ~(size_t)255);
+    L.off_hpre = L.off_hids + (((size_t)L.heavy_cap * nplans * 4 + 255) & ~(size_t)255);
+    L.bytes = L.off_hpre + (((size_t)L.heavy_cap * nplans * 8 + 255) & ~(size_t)255);
     if (o.time_budget_s > 0) L.deadline = std::max<unsigned long long>(1, (unsigned long long)(o.time_budget_s * 1e9));
     return SGE_OK;
 }
@@ -2087,19 +2152,25 @@ sge_status enqueue_launch(sge_graph *g, const LaunchCfg &L, unsigned char *B, ui
     unsigned long long *dqueue = reinterpret_cast<unsigned long long *>(B + L.off_queue);
     uint32_t *dflags = reinterpret_cast<uint32_t *>(B + L.off_flags);
     DevStats *dstats = reinterpret_cast<DevStats *>(B + L.off_stats);
-    uint32_t *dhcnt = reinterpret_cast<uint32_t *>(B + L.off_hcnt);
-    uint32_t *dhids = reinterpret_cast<uint32_t *>(B + L.off_hids);
+    HeavyBuf H{reinterpret_cast<uint32_t *>(B + L.off_hcnt), reinterpret_cast<uint32_t *>(B + L.off_hids),
+               reinterpret_cast<unsigned long long *>(B + L.off_hpre),
+               reinterpret_cast<unsigned long long *>(B + L.off_htot), L.heavy_cap};
     launches = 0;
     for (uint32_t phase = 0; phase < (L.any_split ? 2u : 1u); ++phase) {
-        if (phase == 1) CUDA_TRY(cudaMemsetAsync(dqueue, 0, 8 * (size_t)L.nplans, s));
+        if (phase == 1) {
+            CUDA_TRY(cudaMemsetAsync(dqueue, 0, 8 * (size_t)L.nplans, s));
+            heavy_prefix_kernel<<<L.nplans, 32, 0, s>>>(dg, dplans, L.nplans, H);
+            CUDA_TRY(cudaGetLastError());
+            ++launches;
+        }
         if (L.want_stats)
             count_kernel<true><<<(unsigned)L.blocks, L.threads, L.smem, s>>>(
                 dg, dplans, L.nplans, dqueue, dcounts, scratch, L.cap, L.nbufs, L.tw, L.tmode, L.deadline, dflags,
-                dstats, phase, dhcnt, dhids, L.heavy_cap, L.ntd, L.cs, L.nvs);
+                dstats, phase, H, L.ntd, L.cs, L.nvs);
         else
             count_kernel<false><<<(unsigned)L.blocks, L.threads, L.smem, s>>>(
                 dg, dplans, L.nplans, dqueue, dcounts, scratch, L.cap, L.nbufs, L.tw, L.tmode, L.deadline, dflags,
-                dstats, phase, dhcnt, dhids, L.heavy_cap, L.ntd, L.cs, L.nvs);
+                dstats, phase, H, L.ntd, L.cs, L.nvs);
         CUDA_TRY(cudaGetLastError());
         ++launches;
     }
