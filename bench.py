@@ -1,21 +1,44 @@
 #!/usr/bin/env python3
 """Benchmark of the subgraph-enumeration hot path on GB300.
 
-Workload (the configuration the headline metric is quoted on that fits one
-GPU): a seeded Chung-Lu power-law data graph with n=7,100 vertices, 100,000
-undirected edges, degree exponent 2.1 and maximum degree ~1,000 (uint32 CSR),
-and the query patterns house (5 vertices, 6 edges), K5 minus one edge (9
-edges) and the reference's 8-edge near-5-clique, each planned in the four
-modes WCOJ / exploration (-i) × without / with IEP (-u).  One step = one
-batched persistent launch counting all 12 plans; value = Σ counts / Σ step
-time (embeddings per second in the reference's "Number of matches" units).
+Default workload (the configuration the headline metric is quoted on):
+78 seeded random connected 7-vertex patterns with 16-19 edges
+(PatternGraph.random(7, 16 + i % 4, 2000 + i)) counted on a seeded R-MAT data
+graph with 2^22 vertices and 64M undirected edges (a=.57 b=.19 c=.19, seed 4,
+deduplicated, self-loop-free, ids unpermuted), built on the GPU.  Exact counts
+of these dense patterns over all 64M root edges are beyond any executor (the
+reference needs more than a minute for one of them on a 65K-edge R-MAT), so a
+step counts a fixed root sample: the undirected root edges
+e ≡ SAMPLE_OFFSET (mod SAMPLE_STRIDE) in CSR order, both orientations.  For
+each pattern the planner keeps one symmetry-restriction sequence and one
+root pattern edge (canonical_symmetry), so every plan of a pattern counts
+the same instances on the sample and the two planners below are compared on
+identical counts.
+
+  plain   per pattern: the cost model's plan, then its own launch
+  learned shortlists on host threads, one BF16 MLP scoring call for all 78
+          patterns, one persistent launch of all plans replayed from a CUDA
+          graph (the headline value)
+
+value = Σ sample counts / device time of one batched step (inputs resident in
+HBM); e2e = the same through sge_count_host with the CSR in host memory.
+Counts are the reference's "Number of matches" units (instances: every
+pattern here is a multi-bag plan).
+
+Other workloads: --workload chunglu7100 (a seeded Chung-Lu n=7,100 graph,
+house / K5-e / 8-edge near-5-clique in the four modes WCOJ, WCOJ+IEP,
+exploration, exploration+IEP; full counts), --workload ingest.
 
 Arms:
   --impl sge        (default) the CUDA engine through libsge
-  --impl reference  the CPU implementation of the same path on the host cores
-                    (the oracle port of the reference executor, all threads)
-Under torchrun (N>1) root tasks are sharded across ranks
-(root_stride = world size, root_offset = rank) and per-pattern counts summed.
+  --impl reference  the CPU implementation of the same path on the host cores:
+                    the oracle port of the reference executor with all host
+                    threads, on a bounded sub-sample of the same workload; it
+                    loads only oracle/_build/liboracle.so (graphs from the
+                    oracle's copies of the seeded generators, plans from
+                    tests/golden/bench_plans.npz)
+Under torchrun (N>1) the sampled root edges are sharded across ranks and the
+per-pattern counts summed.
 """
 from __future__ import annotations
 
@@ -33,16 +56,26 @@ REPO = Path(__file__).resolve().parent
 PKG = REPO / "subgraph-enumeration_gb300"
 sys.path.insert(0, str(PKG))
 
-PATTERNS = {
+METRIC = "embeddings/sec on 1 GB300, learned+batched vs plain plan, bit-exact; %HBM peak"
+
+RMAT22 = dict(scale=22, m=64_000_000, a=0.57, b=0.19, c=0.19, seed=4)
+SAMPLE_STRIDE = 1 << 20      # root edges e ≡ SAMPLE_OFFSET (mod SAMPLE_STRIDE)
+SAMPLE_OFFSET = 1
+CPU_SUBSAMPLE = 16           # the CPU runs every CPU_SUBSAMPLE-th edge of the sample
+N_PATTERNS = 78
+
+CL_GRAPH = dict(n=7100, m=100_000, gamma=2.1, max_deg=1000, seed=2)
+CL_PATTERNS = {
     "house": (5, [(0, 1), (0, 2), (0, 4), (1, 3), (1, 4), (2, 3)]),
     "k5_minus_e": (5, [(a, b) for a in range(5) for b in range(a + 1, 5) if (a, b) != (3, 4)]),
     "near5clique_8e": (5, [(0, 1), (0, 2), (0, 3), (0, 4), (1, 2), (1, 3), (1, 4), (2, 3)]),
 }
-MODES = [("wcoj", False, False), ("wcoj-u", False, True), ("explore", True, False), ("explore-u", True, True)]
-GRAPH = dict(n=7100, m=100_000, gamma=2.1, max_deg=1000, seed=2)
+CL_MODES = [("wcoj", False, False), ("wcoj-u", False, True), ("explore", True, False), ("explore-u", True, True)]
 L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
+PLAN_FIXTURE = REPO / "tests" / "golden" / "bench_plans.npz"
 
 
+# ------------------------------------------------------------------ shared ----
 def peaks():
     f = REPO / "MEASURED_PEAKS.json"
     if f.exists():
@@ -51,16 +84,16 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes (read + write) of one count_kernel launch of this workload,
-    from the committed ncu summary (None when it is absent)."""
-    f = REPO / "profiles" / "count_kernel_bench-step_chunglu-n7100.md"
+def profile_traffic(name: str):
+    """DRAM bytes (read + write) of one count_kernel launch of a workload,
+    from its committed ncu summary (None when absent)."""
+    f = REPO / "profiles" / name
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
         if line.startswith("| dram bytes per launch (read + write) |"):
             try:
-                return int(line.split("|")[2].strip())
+                return int(line.split("|")[2].strip().replace(",", ""))
             except ValueError:
                 return None
     return None
@@ -120,48 +153,6 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def build_workload(sge):
-    g = sge.gen_chung_lu(GRAPH["n"], GRAPH["m"], GRAPH["gamma"], GRAPH["max_deg"], GRAPH["seed"])
-    return g
-
-
-def make_plans(sge, stats_or_engine):
-    plans, names = [], []
-    for pname, (k, edges) in PATTERNS.items():
-        p = sge.PatternGraph.from_edges(k, edges)
-        for mname, expl, iep in MODES:
-            plans.append(sge.plan(p, stats_or_engine, iep=iep, exploration=expl))
-            names.append(f"{pname}/{mname}")
-    return plans, names
-
-
-def make_reference_plans(sge, oracle, g, stats, threads):
-    """Plans for the CPU reference arm: the engine's plans, except that for
-    the IEP modes (-u) the cheapest multi-level-tail plan (the reference's
-    inclusion-exclusion leaf) replaces the engine's plan when it is faster on
-    the host, timed on 1/64 of the roots.  The CPU side then runs the better
-    of the two rather than a plan chosen for the GPU."""
-    plans, names = [], []
-    for pname, (k, edges) in PATTERNS.items():
-        p = sge.PatternGraph.from_edges(k, edges)
-        for mname, expl, iep in MODES:
-            b = sge.plan(p, stats, iep=iep, exploration=expl)
-            if iep and b.tail_len < 2:
-                multi = [c for c in sge.candidates(p, stats, iep=True, exploration=expl, cap=4096) if c.tail_len >= 2]
-                if multi:
-                    alt = min(multi, key=lambda c: c.est_cost)
-                    t = []
-                    for cand in (b, alt):
-                        t0 = time.perf_counter()
-                        oracle.count_plan(g.offsets, g.nbrs, cand, threads=threads, stride=64, offset=0)
-                        t.append(time.perf_counter() - t0)
-                    if t[1] < t[0]:
-                        b = alt
-            plans.append(b)
-            names.append(f"{pname}/{mname}")
-    return plans, names
-
-
 def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -169,129 +160,368 @@ def dist_env():
     return world, rank, local
 
 
-def run_reference(args):
-    """CPU arm: the oracle port of the reference executor on the host cores."""
-    world, rank, _ = dist_env()
-    if world > 1 and rank != 0:
-        return
-    sys.path.insert(0, str(REPO / "oracle"))
-    import sge
-    import oracle
-    g = build_workload(sge)
-    st = g.stats()
-    threads = os.cpu_count() or 1
-    plans, names = make_reference_plans(sge, oracle, g, st, threads)
-    # bounded sample: every stride-th root; stride sized for ~10-20 s per step
-    stride = int(os.environ.get("SGE_REF_STRIDE", "8"))
-    def step(offset):
-        t0 = time.perf_counter()
-        total = 0
-        roots = 0
-        for b in plans:
-            inst, done = oracle.count_plan(g.offsets, g.nbrs, b, threads=threads, stride=stride,
-                                           offset=offset % stride)
-            total += inst * b.count_multiplier
-            roots += done
-        return total, time.perf_counter() - t0, roots
-    for w in range(args.warmup):
-        step(w)
-    tot_c, tot_t, roots = 0, 0.0, 0
-    for s in range(args.steps):
-        c, t, r = step(args.warmup + s)
-        tot_c += c
-        tot_t += t
-        roots += r
-    value = tot_c / tot_t
-    line = {"metric": METRIC, "value": value, "unit": "embeddings/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True,
-            "scaling": "strong", "vs_baseline": None, "dtype": "u32 ids / u64 counts", "data": "synthetic",
-            "impl": "reference",
-            "config": workload_config(),
-            "cpu_baseline": {"value": value, "unit": "embeddings/s", "cores": threads, "kind": "port",
-                             "sample": f"1/{stride} of the root edges of each of the 12 plans per step "
-                                       f"({roots} roots over {args.steps} steps), extrapolation-free rate; "
-                                       "IEP modes run the faster on the host of the engine's plan and the "
-                                       "best inclusion-exclusion plan"},
-            "e2e": {"value": value, "unit": "embeddings/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+def canonical_symmetry(k: int, edges) -> tuple[list[int], list[int]]:
+    """The symmetry-restriction sequence and root pattern edge every plan of a
+    pattern keeps: the root is the edge with the largest degree sum (ties:
+    smaller ids), its higher-degree end first; the sequence is the root, then
+    the other vertices by decreasing degree."""
+    E = [(int(a), int(b)) for a, b in edges]
+    deg = [0] * k
+    for a, b in E:
+        deg[a] += 1
+        deg[b] += 1
+    a, b = max(E, key=lambda e: (deg[e[0]] + deg[e[1]], -min(e), -max(e)))
+    if deg[b] > deg[a]:
+        a, b = b, a
+    rest = sorted((v for v in range(k) if v not in (a, b)), key=lambda v: (-deg[v], v))
+    return [a, b] + rest, [a, b]
 
 
-METRIC = "embeddings/sec on 1 GB300 (reference 'Number of matches' units), bit-exact"
+def rmat22_patterns(sge):
+    return [sge.PatternGraph.random(7, 16 + i % 4, 2000 + i) for i in range(N_PATTERNS)]
 
 
-def workload_config():
+def plain_plan(sge, p, st):
+    seq, root = canonical_symmetry(p.k, p.edges)
+    return sge.plan(p, st, symmetry_seq=seq, root_edge=root)
+
+
+def learned_plans(sge, pats, st, mlp, threads: int = 16):
+    """Shortlists (cost model, 64 candidates each, on host threads), one BF16
+    scoring call for every candidate of every pattern, argmin per pattern."""
+    import concurrent.futures as cf
+    import numpy as np
+
+    def shortlist(p):
+        seq, root = canonical_symmetry(p.k, p.edges)
+        sl = sge.candidates(p, st, cap=64, symmetry_seq=seq, root_edge=root)
+        return sl, np.stack([sge.features(b, st) for b in sl])
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(threads, os.cpu_count() or 1))) as ex:
+        res = list(ex.map(shortlist, pats))
+    pred = mlp.forward(np.concatenate([f for _, f in res]), bf16=True)
+    plans, o = [], 0
+    for sl, f in res:
+        plans.append(sl[int(np.argmin(pred[o:o + len(sl)]))])
+        o += len(sl)
+    return plans
+
+
+def sample_opts(world: int = 1, rank: int = 0, sub: int = 1) -> dict:
+    """Root sample of a step (sub > 1: every sub-th edge of it; world > 1:
+    this rank's share).  Edges e ≡ SAMPLE_OFFSET (mod SAMPLE_STRIDE) split as
+    e ≡ SAMPLE_OFFSET + j·SAMPLE_STRIDE (mod SAMPLE_STRIDE·n), j < n."""
+    n = world * sub
+    return dict(root_stride=SAMPLE_STRIDE * n, root_offset=SAMPLE_OFFSET + rank * SAMPLE_STRIDE)
+
+
+def rmat22_config(extra: dict | None = None) -> dict:
+    c = {"workload": f"rmat_s22_m64M x 78 random 7-vertex patterns (16-19 edges), root sample: undirected edges "
+                     f"e = {SAMPLE_OFFSET} mod {SAMPLE_STRIDE} (CSR order, both orientations)",
+         "graph": dict(RMAT22, generator="rmat", ids="unpermuted", built="on the GPU (sge_graph_create_rmat)"),
+         "patterns": "PatternGraph.random(7, 16 + i % 4, 2000 + i), i < 78",
+         "root_sample": {"stride": SAMPLE_STRIDE, "offset": SAMPLE_OFFSET,
+                         "edges": RMAT22["m"] // SAMPLE_STRIDE},
+         "symmetry": "per pattern one restriction sequence and root edge for every plan (canonical_symmetry)",
+         "l2": "inputs larger than L2 (512 MB CSR + 4 GB hub bitmaps); 512 MiB L2 flush before each timed step",
+         "parallelism": "root-edge sharding across ranks"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def chunglu_config() -> dict:
     return {"workload": "chunglu_n7100_m100k_g2.1 x {house, k5_minus_e, near5clique_8e} x "
-                        "{wcoj, wcoj-u, explore, explore-u}",
-            "graph": dict(GRAPH, generator="chung_lu"), "patterns": list(PATTERNS), "plans_per_step": 12,
+                        "{wcoj, wcoj-u, explore, explore-u}, full counts",
+            "graph": dict(CL_GRAPH, generator="chung_lu"), "patterns": list(CL_PATTERNS), "plans_per_step": 12,
             "l2": "flushed between timed steps (512 MiB write); the 0.8 MB CSR itself is L2-resident",
             "parallelism": "root-edge sharding across ranks"}
 
 
-def cpu_sample(oracle, g, plans, stride, offset, threads):
-    t0 = time.perf_counter()
-    total = roots = 0
-    for b in plans:
-        inst, done = oracle.count_plan(g.offsets, g.nbrs, b, threads=threads, stride=stride, offset=offset)
-        total += inst * b.count_multiplier
-        roots += done
-    return total, time.perf_counter() - t0, roots
+def native_loaded() -> list | None:
+    """This repository's shared libraries mapped into the process."""
+    try:
+        maps = Path("/proc/self/maps").read_text().splitlines()
+    except OSError:
+        return None
+    found = set()
+    for ln in maps:
+        path = ln.split()[-1] if ln.split() else ""
+        if path.endswith(".so") and path.startswith(str(REPO) + "/"):
+            found.add(path[len(str(REPO)) + 1:])
+    return sorted(found)
 
 
-def cpu_baseline(sge, g, plans, budget_s=15.0):
-    """The oracle port on all host cores over the same root sample of every
-    pattern and mode of the step (every stride-th root edge), the stride
-    shrunk until the sample takes about budget_s/3 .. budget_s seconds.  The
-    plans are the reference arm's: the engine's, or for the IEP modes the best
-    inclusion-exclusion plan when that is faster on the host."""
+# ------------------------------------------------------- reference (CPU) arm ----
+def oracle_graph(name: str):
+    """Data graph of a workload built by the oracle's copies of the seeded
+    generators (the reference arm never loads the library)."""
+    sys.path.insert(0, str(REPO / "oracle"))
+    import oracle
+    if name == "rmat22":
+        g = RMAT22
+        return oracle.gen_rmat(g["scale"], g["m"], g["a"], g["b"], g["c"], g["seed"])
+    g = CL_GRAPH
+    return oracle.gen_chung_lu(g["n"], g["m"], g["gamma"], g["max_deg"], g["seed"])
+
+
+def fixture_plans(key: str):
+    import numpy as np
+    d = np.load(PLAN_FIXTURE)
+    return d[key]
+
+
+def blob_multiplier(blob) -> int:
+    """count_multiplier of a raw sge_plan_blob (layout of include/sge.h)."""
+    import numpy as np
+    # magic, abi, k, num_enum, tail_mode, tail_len, join_style, root_kind: 8 u32;
+    # 8 arrays of SGE_MAX_K u32; num_partitions; 15 i32; 15 u32; 15x4 u32; then u64
+    off = 4 * (8 + 8 * 16 + 1 + 15 + 15 + 60)
+    off = (off + 7) & ~7
+    return int(np.frombuffer(bytes(blob[off:off + 8]), np.uint64)[0])
+
+
+def run_reference(args):
+    """The CPU implementation of the path (the oracle port of the reference
+    executor, every host thread) on a bounded sample of the workload."""
+    world, rank, _ = dist_env()
+    if world > 1 and rank != 0:
+        return
     sys.path.insert(0, str(REPO / "oracle"))
     import oracle
     threads = os.cpu_count() or 1
-    plans, _ = make_reference_plans(sge, oracle, g, g.stats(), threads)
-    stride = 1 << 14
-    while True:
-        total, dt, roots = cpu_sample(oracle, g, plans, stride, 7 % stride, threads)
-        if dt >= budget_s / 3 or stride == 1:
-            break
-        # aim at budget_s/2, never shrinking the stride by more than 16x per step
-        stride = max(1, stride // max(2, min(16, int(budget_s / 2 / max(dt, 1e-3)))))
-    return {"value": total / dt, "unit": "embeddings/s", "cores": threads, "kind": "port",
-            "sample": f"root edges t = {7 % stride} mod {stride} of all {len(plans)} plans of a step ({roots} roots, "
-                      f"{dt:.1f} s); value = embeddings of the sample / its time; IEP modes run the faster on the "
-                      "host of the engine's plan and the best inclusion-exclusion plan"}
+    t0 = time.perf_counter()
+    off, nb = oracle_graph(args.workload)
+    setup_s = time.perf_counter() - t0
+    if args.workload == "rmat22":
+        blobs = fixture_plans("rmat22_plain")
+        sub = dict(stride=SAMPLE_STRIDE * CPU_SUBSAMPLE, offset=SAMPLE_OFFSET)
+        names = [f"pattern{i}" for i in range(len(blobs))]
+        sample_desc = (f"undirected root edges e = {SAMPLE_OFFSET} mod {SAMPLE_STRIDE * CPU_SUBSAMPLE} (every "
+                       f"{CPU_SUBSAMPLE}th edge of the GPU's sample) of all 78 patterns per step, the cost model's plans "
+                       "with the same symmetry as the GPU's")
+        config = rmat22_config()
+    else:
+        plans = fixture_plans("chunglu7100_plans")
+        alts = fixture_plans("chunglu7100_alt")
+        # the IEP modes run whichever of the engine's plan and the best
+        # inclusion-exclusion plan is faster on these cores (timed on 1/64)
+        blobs = []
+        for b, a in zip(plans, alts):
+            if bytes(a) == bytes(b):
+                blobs.append(b)
+                continue
+            t = []
+            for cand in (b, a):
+                s = time.perf_counter()
+                oracle.count_plans(off, nb, bytes(cand), 1, threads=threads, stride=64, offset=0)
+                t.append(time.perf_counter() - s)
+            blobs.append(a if t[1] < t[0] else b)
+        names = [str(x) for x in fixture_plans("chunglu7100_names")]
+        sub = dict(stride=8, offset=0)
+        sample_desc = ("undirected root edges e = 0 mod 8 of all 12 plans per step; IEP modes run the faster on "
+                       "the host of the engine's plan and the best inclusion-exclusion plan")
+        config = chunglu_config()
+    raw = b"".join(bytes(b) for b in blobs)
+    mult = [blob_multiplier(b) for b in blobs]
+
+    def step():
+        s = time.perf_counter()
+        inst, roots = oracle.count_plans(off, nb, raw, len(blobs), threads=threads, **sub)
+        return sum(i * m for i, m in zip(inst, mult)) % (1 << 64), time.perf_counter() - s, sum(roots)
+    for _ in range(args.warmup):
+        step()
+    tot_c, tot_t, tot_r = 0, 0.0, 0
+    for _ in range(args.steps):
+        c, t, r = step()
+        tot_c += c
+        tot_t += t
+        tot_r += r
+    value = tot_c / tot_t
+    line = {"metric": METRIC, "value": value, "unit": "embeddings/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True,
+            "scaling": "strong", "vs_baseline": None, "dtype": "u32 ids / u64 counts", "data": "synthetic",
+            "impl": "reference", "config": config,
+            "cpu_baseline": {"value": value, "unit": "embeddings/s", "cores": threads, "kind": "port",
+                             "sample": f"{sample_desc} ({tot_r} root tasks over {args.steps} steps)"},
+            "e2e": {"value": value, "unit": "embeddings/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "setup_s": setup_s, "native_loaded": native_loaded()}
+    print(json.dumps(line), flush=True)
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="sge", choices=["sge", "reference"])
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--plans", default="", help="comma-separated subset, e.g. house/wcoj-u (profiling)")
-    ap.add_argument("--per-plan", action="store_true", help="time each plan alone and print one JSON per plan")
-    ap.add_argument("--workload", default="chunglu7100", choices=["chunglu7100", "batch7", "ingest"],
-                    help="batch7: 78 random 7-vertex patterns, learned+batched vs plain planning; "
-                         "ingest: R-MAT 2^20 vertices / 16M edges generated and built on the GPU vs the host "
-                         "(separate lines)")
-    args = ap.parse_args()
-    if args.impl == "reference":
-        return run_reference(args)
-    if args.workload == "batch7":
-        return run_batch7(args)
-    if args.workload == "ingest":
-        return run_ingest(args)
-    world, rank, local = dist_env()
+# ------------------------------------------------------------ GPU arm ----
+def cpu_port_check(off, nb, plans, gpu_sub_counts, sub: dict, budget_s: float = 30.0) -> dict:
+    """The oracle port on every host core over a sub-sample of the step's
+    roots, with the step's own plans: its rate is the CPU baseline, and its
+    counts must equal the GPU's on the same sub-sample."""
+    sys.path.insert(0, str(REPO / "oracle"))
+    import oracle
+    threads = os.cpu_count() or 1
+    raw = b"".join(b.to_bytes() for b in plans)
+    t0 = time.perf_counter()
+    inst, roots = oracle.count_plans(off, nb, raw, len(plans), threads=threads, **sub)
+    dt = time.perf_counter() - t0
+    cpu = [i * b.count_multiplier % (1 << 64) for i, b in zip(inst, plans)]
+    return {"value": sum(cpu) / dt, "unit": "embeddings/s", "cores": threads, "kind": "port",
+            "sample": f"undirected root edges e = {sub['root_offset']} mod {sub['root_stride']} of all "
+                      f"{len(plans)} plans ({sum(roots)} root tasks, {dt:.1f} s); value = embeddings of the "
+                      "sample / its time",
+            "parity_with_gpu": cpu == list(gpu_sub_counts), "seconds": dt}
+
+
+def run_rmat22(args):
+    import numpy as np
     import torch
     import sge
+    import sge_learn
+    world, rank, local = dist_env()
     dist = None
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     device = local if torch.cuda.is_available() else 0
     torch.cuda.set_device(device)
-    g = build_workload(sge)
+    g = RMAT22
+    t0 = time.perf_counter()
+    eng = sge.Engine.rmat_device(g["scale"], g["m"], g["a"], g["b"], g["c"], g["seed"], device=device)
+    ingest_s = time.perf_counter() - t0
+    info = eng.info()
+    st = eng.graph.stats()
+    pats = rmat22_patterns(sge)
+    mlp = sge_learn.load_mlp()
+    shard = sample_opts(world, rank)
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def plain():
+        tw = time.perf_counter()
+        counts, plan_s, kern = [], 0.0, 0.0
+        for p in pats:
+            a = time.perf_counter()
+            b = plain_plan(sge, p, st)
+            plan_s += time.perf_counter() - a
+            c, _, s = eng.count([b], **shard)
+            kern += s["kernel_ms"]
+            counts.append(c[0])
+        return counts, time.perf_counter() - tw, plan_s, kern
+
+    def learned():
+        tw = time.perf_counter()
+        plans = learned_plans(sge, pats, st, mlp)
+        plan_s = time.perf_counter() - tw
+        with eng.batch(plans, **shard) as bt:
+            c, _, s = bt.run()
+        return plans, c, time.perf_counter() - tw, plan_s, s["kernel_ms"]
+
+    # warm-up (module load, allocations), then the planners' wall times
+    learned()
+    barrier()
+    plans, cl, lw, lp, lk = learned()
+    barrier()
+    cp, pw, pp, pk = plain()
+    barrier()
+    assert cp == cl, "plain and learned plans disagree on the sample"
+    # timed steps: replays of the learned batch (CUDA graph), L2 flushed before each
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=f"cuda:{device}")
+    batch = eng.batch(plans, **shard)
+    for _ in range(args.warmup):
+        batch.run()
+    kernel_ms, launches, counts = [], 0, None
+    with ClockSampler(device) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1)
+            barrier()
+            c, _, s = batch.run()
+            barrier()
+            kernel_ms.append(s["kernel_ms"])
+            launches += s["gpu_launches"]
+            counts = c
+    batch.close()
+    # untimed: algorithmic bytes of one step (instrumented kernel) and the
+    # same step without hub bitmaps
+    _, _, sst = eng.count(plans, stats=True, **shard)
+    _, _, snh = eng.count(plans, hub_bitmaps=False, **shard)
+    if dist:
+        tc = torch.tensor([x % (1 << 63) for x in counts], dtype=torch.int64, device=f"cuda:{device}")
+        dist.all_reduce(tc)
+        counts_all = [int(x) for x in tc.tolist()]
+        tk = torch.tensor([sum(kernel_ms)], dtype=torch.float64, device=f"cuda:{device}")
+        dist.all_reduce(tk, op=dist.ReduceOp.MAX)
+        sum_k = float(tk.item())
+    else:
+        counts_all, sum_k = counts, sum(kernel_ms)
+    total = sum(counts_all)
+    avg_s = sum_k / len(kernel_ms) / 1e3
+    value = total / avg_s
+    # e2e through the C ABI with the CSR in host memory (upload, root list,
+    # hub index, count and read-back inside the timed region)
+    e2e_ms = []
+    for _ in range(max(1, min(args.steps, 2))):
+        barrier()
+        t = time.perf_counter()
+        ec, _ = sge.count_host(eng.graph, plans, **shard)
+        e2e_ms.append((time.perf_counter() - t) * 1e3)
+        assert ec == counts
+    e2e_value = sum(counts) / (statistics.median(e2e_ms) / 1e3)
+    h2d = 4 * (info["num_vertices"] + 1) + 4 * info["num_directed_edges"] + 4 * info["num_directed_edges"] + \
+        len(plans[0].to_bytes()) * len(plans)
+    d2h = 8 * len(plans) + 4
+    peak, peak_kind = peaks()
+    achieved = sst["alg_bytes"] / avg_s / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "embeddings/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sum_k / len(kernel_ms), "higher_is_better": True,
+        "scaling": "strong", "vs_baseline": None, "dtype": "u32 ids / u64 counts", "data": "synthetic",
+        "config": rmat22_config({"ingest_s": ingest_s, "hub_index": {"hubs": info["hub_count"],
+                                                                      "min_degree": info["hub_min_degree"]},
+                                 "max_degree": info["max_degree"]}),
+        "learned_batched": {"wall_s": lw, "planning_s": lp, "kernel_ms": lk, "value_wall": total / lw},
+        "plain": {"wall_s": pw, "planning_s": pp, "kernel_ms": pk, "value_wall": total / pw,
+                  "launches": len(pats)},
+        "speedup_wall": pw / lw, "speedup_kernel": pk / lk,
+        "kernel_ms_without_hub_bitmaps": snh["kernel_ms"],
+        "total_count": total,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": profile_traffic("count_kernel_rmat22-sample.md"),
+                     "alg_bytes_per_launch": sst["alg_bytes"],
+                     "note": "algorithmic bytes = 4·(base + probed list elements) per set operation + 8 B per CSR "
+                             "offset pair, summed by the instrumented kernel over one step"},
+        "e2e": {"value": e2e_value, "unit": "embeddings/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": statistics.median(e2e_ms)},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sub = sample_opts(1, 0, CPU_SUBSAMPLE)
+        gsub, _, _ = eng.count(plans, **sub)
+        line["cpu_baseline"] = cpu_port_check(eng.graph.offsets, eng.graph.nbrs, plans, gsub, sub)
+    eng.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_chunglu(args):
+    import torch
+    import sge
+    world, rank, local = dist_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    device = local if torch.cuda.is_available() else 0
+    torch.cuda.set_device(device)
+    g = sge.gen_chung_lu(CL_GRAPH["n"], CL_GRAPH["m"], CL_GRAPH["gamma"], CL_GRAPH["max_deg"], CL_GRAPH["seed"])
     eng = sge.Engine(g, device=device)
-    plans, names = make_plans(sge, eng)
+    plans, names = [], []
+    for pname, (k, edges) in CL_PATTERNS.items():
+        p = sge.PatternGraph.from_edges(k, edges)
+        for mname, expl, iep in CL_MODES:
+            plans.append(sge.plan(p, eng, iep=iep, exploration=expl))
+            names.append(f"{pname}/{mname}")
     if args.plans:
         keep = set(args.plans.split(","))
         sel = [i for i, n in enumerate(names) if n in keep]
@@ -303,8 +533,7 @@ def main():
             c2, _, st2 = eng.count([b])
             print(json.dumps({"plan": n, "count": c[0], "kernel_ms": st2["kernel_ms"], "alg_bytes": st["alg_bytes"],
                               "set_ops": st["set_ops"], "partial_matches": st["partial_matches"],
-                              "roots": st["root_tasks"], "stats_kernel_ms": st["kernel_ms"],
-                              "plan_summary": b.summary()}), flush=True)
+                              "roots": st["root_tasks"], "plan_summary": b.summary()}), flush=True)
         eng.close()
         return
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=f"cuda:{device}")
@@ -314,82 +543,79 @@ def main():
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
-
-    # warm-up
     for _ in range(args.warmup):
         eng.count(plans, **shard)
-    # algorithmic bytes of one launch (stats variant, untimed)
     _, _, st = eng.count(plans, stats=True, **shard)
-    alg_bytes = st["alg_bytes"]
-    # timed steps: one replay of the captured batch (CUDA graph) per step, L2
-    # flushed before each; device time from events around the graph launch
-    kernel_ms, host_ms, counts, launches = [], [], None, 0
+    kernel_ms, launches, counts = [], 0, None
     batch = eng.batch(plans, **shard)
     with ClockSampler(device) as clk:
         for _ in range(args.steps):
             flush.fill_(1)
             barrier()
-            t0 = time.perf_counter()
-            c, inst, s = batch.run()
-            t1 = time.perf_counter()
+            c, _, s = batch.run()
             barrier()
             kernel_ms.append(s["kernel_ms"])
-            host_ms.append((t1 - t0) * 1e3)
             launches += s["gpu_launches"]
             counts = c
     batch.close()
-    # reduce over ranks: counts summed, times max
     if dist:
         tc = torch.tensor(counts, dtype=torch.int64, device=f"cuda:{device}")
         dist.all_reduce(tc)
         counts = [int(x) % 2**64 for x in tc.tolist()]
-        tk = torch.tensor([sum(kernel_ms), sum(host_ms)], dtype=torch.float64, device=f"cuda:{device}")
+        tk = torch.tensor([sum(kernel_ms)], dtype=torch.float64, device=f"cuda:{device}")
         dist.all_reduce(tk, op=dist.ReduceOp.MAX)
-        sum_k, sum_h = tk.tolist()
+        sum_k = float(tk.item())
     else:
-        sum_k, sum_h = sum(kernel_ms), sum(host_ms)
-    total_count = sum(counts)
-    value = total_count * args.steps / (sum_k / 1e3)
-    # e2e: host buffers through the C ABI (H2D, count, D2H inside the timed region)
+        sum_k = sum(kernel_ms)
+    total = sum(counts)
+    value = total * args.steps / (sum_k / 1e3)
     e2e_ms = []
     for _ in range(max(2, min(args.steps, 5))):
         barrier()
         t0 = time.perf_counter()
-        ec, est = sge.count_host(g, plans, stats=False)
+        ec, _ = sge.count_host(g, plans)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
         assert ec == counts or world > 1
-    e2e_value = total_count / (statistics.median(e2e_ms) / 1e3)
-    h2d = 4 * (g.num_vertices + 1) + 4 * g.nbrs.size + 8 * g.num_edges + 300 * len(plans)
+    e2e_value = total / (statistics.median(e2e_ms) / 1e3)
+    h2d = 4 * (g.num_vertices + 1) + 4 * g.nbrs.size + 8 * g.num_edges + len(plans[0].to_bytes()) * len(plans)
     d2h = 8 * len(plans) + 4
-    peak, peak_kind = peaks()
-    avg_launch_s = sum_k / len(kernel_ms) / 1e3
-    achieved = alg_bytes / avg_launch_s / 1e9
-    traffic = profile_traffic()
+    avg_s = sum_k / len(kernel_ms) / 1e3
     line = {
         "metric": METRIC, "value": value, "unit": "embeddings/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sum_k / len(kernel_ms), "higher_is_better": True,
         "scaling": "strong", "vs_baseline": None, "dtype": "u32 ids / u64 counts", "data": "synthetic",
-        "config": workload_config(),
-        "counts": dict(zip(names, counts)),
-        "host_ms_per_step": sum_h / len(host_ms),
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": traffic,
-                     "alg_bytes_per_launch": alg_bytes,
-                     "note": "algorithmic bytes = 4·(base + probed list elements) per set operation + 8 B per "
-                             "CSR offset pair; the CSR is L2-resident at this size"},
+        "config": chunglu_config(), "counts": dict(zip(names, counts)),
+        "roofline": {"bound": "l2/latency", "achieved": st["alg_bytes"] / avg_s / 1e9, "unit": "GB/s",
+                     "alg_bytes_per_launch": st["alg_bytes"], "l2_hit_rate": profile_l2_hit(),
+                     "traffic": profile_traffic("count_kernel_bench-step_chunglu-n7100.md"),
+                     "note": "the 0.8 MB CSR and its hub bitmaps stay in L2, so the kernel is bound by L2/shared-"
+                             "memory latency of the dependent probes; no HBM fraction is claimed"},
         "e2e": {"value": e2e_value, "unit": "embeddings/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": statistics.median(e2e_ms)},
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(sge, g, plans)
+        gsub, _, _ = eng.count(plans, root_stride=8, root_offset=0)
+        line["cpu_baseline"] = cpu_port_check(g.offsets, g.nbrs, plans, gsub, dict(root_stride=8, root_offset=0))
     eng.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def profile_l2_hit():
+    f = REPO / "profiles" / "count_kernel_bench-step_chunglu-n7100.md"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("| lts__t_sector_hit_rate"):
+            try:
+                return float(line.split("|")[2].strip().rstrip("%")) / 100.0
+            except ValueError:
+                return None
+    return None
 
 
 INGEST_GRAPH = dict(scale=20, m=16_000_000, a=0.57, b=0.19, c=0.19, seed=11)
@@ -425,99 +651,30 @@ def run_ingest(args):
             "data": "synthetic", "dtype": "u32 ids",
             "config": {"workload": "rmat_s20_m16M ingest", "graph": dict(gs, generator="rmat"),
                        "directed_edges": int(nb.size), "csr_identical_to_host": True,
-                       "device_path": "sge_graph_create_rmat (includes the host copy used for planner statistics)",
+                       "device_path": "sge_graph_create_rmat (includes the host copy used for planner statistics "
+                                      "and the hub index)",
                        "host_path": "sge_gen_rmat + sge_csr_from_edges + sge_graph_create (validation, upload)"}}
     print(json.dumps(line), flush=True)
 
 
-BATCH7_GRAPH = dict(scale=10, m=8000, a=0.57, b=0.19, c=0.19, seed=4)
-
-
-def run_batch7(args):
-    """Learned + batched vs plain planning on a batch of 78 seeded random
-    7-vertex patterns (16-19 edges) over a seeded R-MAT graph (scale 10,
-    8,000 edges: the batch configuration's generator at a size whose exact
-    counts finish in seconds).  Wall time includes planning.
-      plain:   per pattern, cost-model plan then its own launch (as the
-               reference runs one process per pattern)
-      learned: shortlists on host threads, one BF16 MLP scoring call for all
-               patterns, one launch of all plans replayed from a CUDA graph."""
-    import concurrent.futures as cf
-    import numpy as np
-    import torch
-    import sge
-    import sge_learn
-    gs = BATCH7_GRAPH
-    g = sge.gen_rmat(gs["scale"], gs["m"], gs["a"], gs["b"], gs["c"], gs["seed"])
-    pats = [sge.PatternGraph.random(7, 16 + i % 4, 2000 + i) for i in range(78)]
-    eng = sge.Engine(g)
-    st = g.stats()
-    mlp = sge_learn.load_mlp()
-
-    def plain():
-        t0 = time.perf_counter()
-        counts, plan_s, kern = [], 0.0, 0.0
-        for p in pats:
-            a = time.perf_counter()
-            b = sge.plan(p, st)
-            plan_s += time.perf_counter() - a
-            c, _, s = eng.count([b])
-            kern += s["kernel_ms"]
-            counts.append(c[0])
-        return counts, time.perf_counter() - t0, plan_s, kern
-
-    def learned():
-        t0 = time.perf_counter()
-        with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
-            shortlists = list(ex.map(lambda p: sge.candidates(p, st, cap=64), pats))
-        feats = np.concatenate([np.stack([sge.features(b, st) for b in sl]) for sl in shortlists])
-        pred = mlp.forward(feats, bf16=True)
-        plans, o = [], 0
-        for sl in shortlists:
-            plans.append(sl[int(np.argmin(pred[o:o + len(sl)]))])
-            o += len(sl)
-        plan_s = time.perf_counter() - t0
-        with eng.batch(plans) as bt:
-            c, _, s = bt.run()
-        return c, time.perf_counter() - t0, plan_s, s["kernel_ms"]
-
-    for _ in range(args.warmup):
-        learned()
-    pw, lw, pk, lk, pp, lp = [], [], [], [], [], []
-    for _ in range(args.steps):
-        torch.cuda.synchronize()
-        cp, tp, plan_p, kp = plain()
-        cl, tl, plan_l, kl = learned()
-        assert cp == cl, "plain and learned plans disagree"
-        pw.append(tp); lw.append(tl); pk.append(kp); lk.append(kl); pp.append(plan_p); lp.append(plan_l)
-    total = sum(cl)
-    # the same learned plans with no heavy-root splitting (one launch, a warp per root)
-    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
-        shortlists = list(ex.map(lambda p: sge.candidates(p, st, cap=64), pats))
-    feats = np.concatenate([np.stack([sge.features(b, st) for b in sl]) for sl in shortlists])
-    pred = mlp.forward(feats, bf16=True)
-    plans, o = [], 0
-    for sl in shortlists:
-        plans.append(sl[int(np.argmin(pred[o:o + len(sl)]))])
-        o += len(sl)
-    with eng.batch(plans, heavy_threshold=1 << 30) as bt:
-        cn, _, sn = bt.run()
-    assert cn == cl
-    line = {"metric": "embeddings/sec, learned+batched planning and execution (wall time incl. planning)",
-            "value": total / statistics.median(lw), "unit": "embeddings/s", "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(lw), "higher_is_better": True,
-            "scaling": "strong", "vs_baseline": None, "dtype": "u32 ids / u64 counts", "data": "synthetic",
-            "config": {"workload": "rmat_s10_m8000 x 78 random 7-vertex patterns (16-19 edges)",
-                       "graph": dict(gs, generator="rmat"), "patterns": "PatternGraph.random(7, 16 + i%4, 2000 + i)"},
-            "learned_batched": {"wall_s": statistics.median(lw), "planning_s": statistics.median(lp),
-                                "kernel_ms": statistics.median(lk), "kernel_ms_without_root_split": sn["kernel_ms"]},
-            "plain": {"wall_s": statistics.median(pw), "planning_s": statistics.median(pp),
-                      "kernel_ms": statistics.median(pk), "value": total / statistics.median(pw)},
-            "speedup_wall": statistics.median(pw) / statistics.median(lw),
-            "speedup_kernel": statistics.median(pk) / statistics.median(lk),
-            "total_count": total}
-    eng.close()
-    print(json.dumps(line), flush=True)
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="sge", choices=["sge", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="rmat22", choices=["rmat22", "chunglu7100", "ingest"])
+    ap.add_argument("--plans", default="", help="chunglu7100: comma-separated subset, e.g. house/wcoj-u")
+    ap.add_argument("--per-plan", action="store_true", help="chunglu7100: time each plan alone")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.workload == "ingest":
+        return run_ingest(args)
+    if args.workload == "chunglu7100":
+        return run_chunglu(args)
+    return run_rmat22(args)
 
 
 if __name__ == "__main__":

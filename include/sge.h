@@ -173,6 +173,8 @@ typedef struct sge_count_opts {
                                    quarter as many per extra level) run by a second launch */
     uint32_t no_hub_bitmaps;    /* 1: probe every adjacency list by binary search, ignoring the graph's
                                    hub bitmaps (for comparison runs); 0 = use them */
+    uint32_t root_max_degree;   /* 0 = every sampled root; d > 0: only roots whose two endpoints both have
+                                   degree <= d (a bounded sub-sample, e.g. for a CPU check) */
 } sge_count_opts;
 
 /* Statistics of one sge_count call (per call, summed over plans).  kernel_ms,

@@ -45,7 +45,8 @@ def lib() -> C.CDLL:
         L.oracle_count_plan.restype = u64
         L.oracle_count_plan.argtypes = [_P(u32), _P(u32), u32, C.c_void_p, C.c_int, u64, u64, _P(u64)]
         L.oracle_count_plans.restype = None
-        L.oracle_count_plans.argtypes = [_P(u32), _P(u32), u32, C.c_void_p, u32, C.c_int, u64, u64, _P(u64), _P(u64)]
+        L.oracle_count_plans.argtypes = [_P(u32), _P(u32), u32, C.c_void_p, u32, C.c_int, u64, u64, u32, _P(u64),
+                                         _P(u64)]
         L.oracle_max_threads.restype = C.c_int
         L.oracle_list_embeddings.restype = u64
         L.oracle_list_embeddings.argtypes = [_P(u32), _P(u32), u32, u32, u32, _P(u32), _P(u32), u64]
@@ -131,16 +132,17 @@ def count_plan(offsets, nbrs, blob, threads: int = 0, stride: int = 1, offset: i
 
 
 def count_plans(offsets, nbrs, blobs: bytes, nplans: int, threads: int = 0, stride: int = 1,
-                offset: int = 0) -> tuple[list[int], list[int]]:
+                offset: int = 0, root_max_degree: int = 0) -> tuple[list[int], list[int]]:
     """Runs nplans plan blobs (their raw bytes back to back) over the same root
-    sample (undirected edges e ≡ offset mod stride).  Returns (instances per
-    plan, root tasks per plan)."""
+    sample (undirected edges e ≡ offset mod stride; root_max_degree > 0 keeps
+    the roots whose endpoints both have at most that degree).  Returns
+    (instances per plan, root tasks per plan)."""
     off, nb = _arr(offsets), _arr(nbrs)
     buf = C.create_string_buffer(bytes(blobs), len(blobs))
     counts = (u64 * nplans)()
     roots = (u64 * nplans)()
     lib().oracle_count_plans(_p(off), _p(nb), off.size - 1, C.addressof(buf), nplans, threads, stride, offset,
-                             counts, roots)
+                             root_max_degree, counts, roots)
     return [int(x) for x in counts], [int(x) for x in roots]
 
 

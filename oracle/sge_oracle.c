@@ -461,7 +461,7 @@ static uint64_t tail_count(const exec_ctx *c, const uint32_t *mm, uint32_t **buf
  * reference's number). */
 static uint64_t count_plan_roots(const uint32_t *off, const uint32_t *nb, uint32_t maxdeg, const uint32_t *eu,
                                  const uint32_t *ev, uint64_t m, const sge_plan_blob *p, int threads, uint64_t stride,
-                                 uint64_t offset, uint64_t *roots_done);
+                                 uint64_t offset, uint32_t root_max_degree, uint64_t *roots_done);
 
 /* Root edges u<v in CSR order (the engine's root-task numbering). */
 static uint64_t root_edges(const uint32_t *off, const uint32_t *nb, uint32_t n, uint32_t **eu, uint32_t **ev,
@@ -481,7 +481,7 @@ uint64_t oracle_count_plan(const uint32_t *off, const uint32_t *nb, uint32_t n, 
                            uint64_t stride, uint64_t offset, uint64_t *roots_done) {
     uint32_t *eu, *ev, maxdeg;
     const uint64_t m = root_edges(off, nb, n, &eu, &ev, &maxdeg);
-    const uint64_t r = count_plan_roots(off, nb, maxdeg, eu, ev, m, p, threads, stride, offset, roots_done);
+    const uint64_t r = count_plan_roots(off, nb, maxdeg, eu, ev, m, p, threads, stride, offset, 0, roots_done);
     free(eu);
     free(ev);
     return r;
@@ -489,34 +489,84 @@ uint64_t oracle_count_plan(const uint32_t *off, const uint32_t *nb, uint32_t n, 
 
 /* Several plans over the same root sample, the root list built once:
  * counts[i] = instances of plan i over the sampled roots, roots[i] = the
- * root tasks it ran. */
+ * root tasks it ran.  root_max_degree > 0 keeps only the roots whose two
+ * endpoints both have at most that degree. */
 void oracle_count_plans(const uint32_t *off, const uint32_t *nb, uint32_t n, const sge_plan_blob *plans,
-                        uint32_t nplans, int threads, uint64_t stride, uint64_t offset, uint64_t *counts,
-                        uint64_t *roots) {
+                        uint32_t nplans, int threads, uint64_t stride, uint64_t offset, uint32_t root_max_degree,
+                        uint64_t *counts, uint64_t *roots) {
     uint32_t *eu, *ev, maxdeg;
     const uint64_t m = root_edges(off, nb, n, &eu, &ev, &maxdeg);
     for (uint32_t i = 0; i < nplans; ++i)
-        counts[i] = count_plan_roots(off, nb, maxdeg, eu, ev, m, &plans[i], threads, stride, offset, &roots[i]);
+        counts[i] = count_plan_roots(off, nb, maxdeg, eu, ev, m, &plans[i], threads, stride, offset, root_max_degree,
+                                     &roots[i]);
     free(eu);
     free(ev);
 }
 
 /* Runs plan p over the sampled undirected root edges e ≡ offset (mod stride)
- * (both orientations when the root is unordered). */
+ * (both orientations when the root is unordered), in parallel like
+ * parSharedJoin (matching/parallel.cpp:1154-1486), with one refinement: a root
+ * with more than 64 level-2 candidates is split into up to 64 work items over
+ * ranges of them, so one heavy root does not hold a single thread while the
+ * others idle.  The counts are the same; only the CPU's time is shorter. */
 static uint64_t count_plan_roots(const uint32_t *off, const uint32_t *nb, uint32_t maxdeg, const uint32_t *eu,
                                  const uint32_t *ev, uint64_t m, const sge_plan_blob *p, int threads, uint64_t stride,
-                                 uint64_t offset, uint64_t *roots_done) {
+                                 uint64_t offset, uint32_t root_max_degree, uint64_t *roots_done) {
     exec_ctx c;
     c.off = off; c.nb = nb; c.p = p; c.maxdeg = maxdeg;
     const int64_t nor = (p->root_kind == SGE_ROOT_ANY) ? 2 : 1;
     if (stride == 0) stride = 1;
-    uint64_t total = 0, done = 0;
+    const uint32_t K = p->k, ne = p->num_enum;
+    const int64_t nedge = offset < m ? (int64_t)((m - offset + stride - 1) / stride) : 0;
+    const int64_t nroot = nedge * nor;
 #ifdef _OPENMP
     if (threads > 0) omp_set_num_threads(threads);
+#endif
+    /* the root task r -> (a, b) */
+    #define ROOT_OF(r, a, b) do { \
+        const uint64_t ei_ = offset + (uint64_t)((r) / nor) * stride; \
+        a = eu[ei_]; b = ev[ei_]; \
+        if ((p->root_kind == SGE_ROOT_ANY && ((r) % nor) == 1) || p->root_kind == SGE_ROOT_DESC) { uint32_t x_ = a; a = b; b = x_; } \
+    } while (0)
+    /* pass A: each root's level-2 list size and its number of work items */
+    uint64_t *pre = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)(nroot + 1));
+    uint32_t *c2 = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(nroot + 1));
+#ifdef _OPENMP
+#pragma omp parallel
+#endif
+    {
+        uint32_t *buf = (uint32_t *)malloc(sizeof(uint32_t) * (c.maxdeg + 1));
+        uint32_t *tmp = (uint32_t *)malloc(sizeof(uint32_t) * (c.maxdeg + 1));
+        uint32_t mm[SGE_MAX_K];
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 256)
+#endif
+        for (int64_t r = 0; r < nroot; ++r) {
+            uint32_t a, b;
+            ROOT_OF(r, a, b);
+            if (root_max_degree && (off[a + 1] - off[a] > root_max_degree || off[b + 1] - off[b] > root_max_degree)) {
+                c2[r] = 0xFFFFFFFFu;  /* dropped by the degree cap */
+                continue;
+            }
+            if (ne == 2) { c2[r] = 0; continue; }
+            mm[0] = a; mm[1] = b;
+            c2[r] = level_candidates(&c, 2, mm, buf, tmp);
+        }
+        free(buf);
+        free(tmp);
+    }
+    pre[0] = 0;
+    for (int64_t r = 0; r < nroot; ++r) {
+        const uint32_t n2 = c2[r];
+        const uint64_t items = n2 == 0xFFFFFFFFu ? 0u : n2 <= 64 ? 1u : (n2 / 16 < 64 ? n2 / 16 : 64);
+        pre[r + 1] = pre[r] + items;
+    }
+    const int64_t nitems = (int64_t)pre[nroot];
+    uint64_t total = 0, done = 0;
+#ifdef _OPENMP
 #pragma omp parallel reduction(+ : total, done)
 #endif
     {
-        const uint32_t K = p->k, ne = p->num_enum;
         uint32_t *bufs[SGE_MAX_K + SGE_MAX_TAIL];
         for (uint32_t i = 0; i < SGE_MAX_K + SGE_MAX_TAIL; ++i) bufs[i] = (uint32_t *)malloc(sizeof(uint32_t) * (c.maxdeg + 1));
         uint32_t *tmp = (uint32_t *)malloc(sizeof(uint32_t) * (c.maxdeg + 1));
@@ -528,22 +578,26 @@ static uint64_t count_plan_roots(const uint32_t *off, const uint32_t *nb, uint32
         }
         for (uint32_t i = ne; i < K; ++i)
             if (hoisted_level(p, i)) hoist[i] = (uint32_t *)malloc(sizeof(uint32_t) * (c.maxdeg + 1));
-        (void)K;
 #ifdef _OPENMP
-#pragma omp for schedule(dynamic, 64)
+#pragma omp for schedule(dynamic, 16)
 #endif
-        for (int64_t ei = (int64_t)offset; ei < (int64_t)m; ei += (int64_t)stride) {
-          for (int64_t o = 0; o < nor; ++o) {
-            uint32_t a = eu[ei], b = ev[ei];
-            if ((p->root_kind == SGE_ROOT_ANY && o == 1) || p->root_kind == SGE_ROOT_DESC) { uint32_t x = a; a = b; b = x; }
+        for (int64_t q = 0; q < nitems; ++q) {
+            /* the root holding item q: the last r with pre[r] <= q */
+            int64_t lo = 0, hi = nroot;
+            while (hi - lo > 1) { const int64_t mid = (lo + hi) / 2; if (pre[mid] <= (uint64_t)q) lo = mid; else hi = mid; }
+            const int64_t r = lo;
+            const uint64_t part = (uint64_t)q - pre[r], parts = pre[r + 1] - pre[r];
+            uint32_t a, b;
+            ROOT_OF(r, a, b);
             mm[0] = a; mm[1] = b;
-            ++done;
+            if (part == 0) ++done;
             if (ne == 2) { total += tail_count(&c, mm, bufs + SGE_MAX_K, tmp, hoist, hoist_n); continue; }
             for (uint32_t i = ne; i < K; ++i)
                 if (hoist[i] && hoist_at_level(p, i) == 1) hoist_n[i] = raw_intersection(&c, i, mm, hoist[i], tmp);
             int lv = 2;
-            cnt[2] = level_candidates(&c, 2, mm, bufs[2], tmp);
-            it[2] = 0;
+            const uint32_t n2 = level_candidates(&c, 2, mm, bufs[2], tmp);
+            it[2] = (uint32_t)((uint64_t)n2 * part / parts);
+            cnt[2] = (uint32_t)((uint64_t)n2 * (part + 1) / parts);
             while (lv >= 2) {
                 if (it[lv] >= cnt[lv]) { --lv; continue; }
                 mm[lv] = bufs[lv][it[lv]++];
@@ -554,12 +608,14 @@ static uint64_t count_plan_roots(const uint32_t *off, const uint32_t *nb, uint32
                 cnt[lv] = level_candidates(&c, (uint32_t)lv, mm, bufs[lv], tmp);
                 it[lv] = 0;
             }
-          }
         }
         for (uint32_t i = 0; i < SGE_MAX_K + SGE_MAX_TAIL; ++i) free(bufs[i]);
         for (uint32_t i = 0; i < SGE_MAX_K; ++i) free(hoist[i]);
         free(tmp);
     }
+    #undef ROOT_OF
+    free(pre);
+    free(c2);
     if (roots_done) *roots_done = done;
     return total;
 }

@@ -93,6 +93,7 @@ struct DevPlan {
     uint32_t epin;                                // exploration: tail level whose root-level running list is pinned
     uint32_t tail_par;                            // union of the tail levels' parents
     uint32_t choose_wrap;                         // CHOOSE leaves use the reference's wrapping choosec
+    uint32_t root_maxdeg;                         // roots with an endpoint of larger degree are skipped (0 = none)
 };
 static_assert(sizeof(DevPlan) % 4 == 0, "DevPlan is copied as 32-bit words");
 
@@ -1478,6 +1479,13 @@ __device__ __forceinline__ uint2 root_edge(const DevGraph &g, const DevPlan &P, 
     return e;
 }
 
+// A root kept by the degree cap: both endpoints of degree <= root_maxdeg.
+__device__ __forceinline__ bool root_kept(const DevGraph &g, const DevPlan &P, uint2 e) {
+    if (!P.root_maxdeg) return true;
+    return __ldg(g.off + e.x + 1) - __ldg(g.off + e.x) <= P.root_maxdeg &&
+           __ldg(g.off + e.y + 1) - __ldg(g.off + e.y) <= P.root_maxdeg;
+}
+
 // Upper bound on a root's level-2 list: the smaller degree among level 2's
 // root parents.
 __device__ __forceinline__ uint32_t level2_bound(const DevGraph &g, const DevPlan &P, uint2 e) {
@@ -1606,20 +1614,33 @@ __global__ void __launch_bounds__(COUNT_MAX_WARPS * 32, 7) count_kernel(DevGraph
             continue;
         }
         if (P.ne == 2) {
-            // lane l takes task t0 + l
+            // lane l takes task t0 + l; roots the degree cap drops are compacted out
             const uint32_t n = (uint32_t)(t1 - t0);
             uint32_t u = 0, v = 0;
+            bool keep = false;
             if (lane < n) {
                 const uint2 e = root_edge(g, P, t0 + lane);
                 u = e.x;
                 v = e.y;
+                keep = root_kept(g, P, e);
             }
-            acc += leaf_roots(P, W, c, n, u, v);
-            roots += n;
+            const uint32_t kb = __ballot_sync(FULL_MASK, keep);
+            const uint32_t nk = __popc(kb);
+            // lane r takes the r-th kept root
+            uint32_t src = 0;
+            {
+                uint32_t msk = kb;
+                for (uint32_t r = 0; r < lane && msk; ++r) msk &= msk - 1;
+                src = msk ? (uint32_t)(__ffs(msk) - 1) : 0u;
+            }
+            const uint32_t ku = __shfl_sync(FULL_MASK, u, src), kv = __shfl_sync(FULL_MASK, v, src);
+            if (nk) acc += leaf_roots(P, W, c, nk, ku, kv);
+            roots += nk;
             continue;
         }
         for (unsigned long long t = t0; t < t1; ++t) {
             const uint2 e = root_edge(g, P, t);
+            if (!root_kept(g, P, e)) continue;
             ++roots;
             if (P.split_S && level2_bound(g, P, e) > P.split_H) {
                 uint32_t slot = 0;
@@ -2049,6 +2070,7 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
     if (g->n <= 32768u) { L.tmode = 1; L.tw = std::max<uint32_t>(32u, ((g->n + 31u) / 32u + 31u) & ~31u); }
     else { L.tmode = 2; L.tw = 512; }
     L.want_stats = o.collect_counters != 0;
+    for (auto &d : L.dps) d.root_maxdeg = o.root_max_degree;
     L.use_hubs = o.no_hub_bitmaps == 0;
     // warps per block: 4 or 2, whichever keeps more warps resident per SM
     // (shared memory per warp is several KB, so smaller blocks pack better)

@@ -80,7 +80,7 @@ class PlanOpts(C.Structure):
 class CountOpts(C.Structure):
     _fields_ = [("blocks_per_sm", u32), ("warps_per_block", u32), ("chunk", u32), ("time_budget_s", C.c_double),
                 ("max_level_capacity", u32), ("root_stride", u64), ("root_offset", u64), ("collect_counters", u32),
-                ("heavy_threshold", u32), ("no_hub_bitmaps", u32)]
+                ("heavy_threshold", u32), ("no_hub_bitmaps", u32), ("root_max_degree", u32)]
 
 
 class Stats(C.Structure):
@@ -560,7 +560,8 @@ class Engine:
 
     def count(self, plans: list[PlanBlob], stats: bool = False, time_budget_s: float = 0.0,
               max_level_capacity: int = 0, blocks_per_sm: int = 0, warps_per_block: int = 0, chunk: int = 0,
-              root_stride: int = 1, root_offset: int = 0, heavy_threshold: int = 0, hub_bitmaps: bool = True):
+              root_stride: int = 1, root_offset: int = 0, heavy_threshold: int = 0, hub_bitmaps: bool = True,
+              root_max_degree: int = 0):
         """Counts every plan over the graph in one launch.  Returns (counts,
         instances, stats-dict); counts are the reference's "Number of matches"
         (uint64).  stats=True runs the instrumented kernel (set operations,
@@ -569,7 +570,8 @@ class Engine:
         t ≡ root_offset (mod root_stride) (sharding, sampling).  heavy_threshold
         (0 = auto) splits roots whose level-2 list may exceed it into tasks of
         a second launch.  hub_bitmaps=False probes every adjacency list by
-        binary search (comparison runs)."""
+        binary search (comparison runs).  root_max_degree > 0 keeps only the
+        sampled roots whose endpoints both have at most that degree."""
         handles = []
         try:
             for b in plans:
@@ -581,7 +583,7 @@ class Engine:
             inst = (u64 * len(plans))()
             st = Stats()
             o = CountOpts(blocks_per_sm, warps_per_block, chunk, time_budget_s, max_level_capacity, root_stride,
-                          root_offset, int(stats), heavy_threshold, int(not hub_bitmaps))
+                          root_offset, int(stats), heavy_threshold, int(not hub_bitmaps), root_max_degree)
             _check(lib().sge_count(self._h, arr, len(plans), C.byref(o), counts, inst, C.byref(st)))
             return list(counts), list(inst), st.as_dict()
         finally:
@@ -635,7 +637,8 @@ class Batch:
 
     def __init__(self, engine: Engine, plans: list[PlanBlob], stats: bool = False, time_budget_s: float = 0.0,
                  blocks_per_sm: int = 0, warps_per_block: int = 0, chunk: int = 0, root_stride: int = 1,
-                 root_offset: int = 0, heavy_threshold: int = 0, hub_bitmaps: bool = True):
+                 root_offset: int = 0, heavy_threshold: int = 0, hub_bitmaps: bool = True,
+                 root_max_degree: int = 0):
         self.engine = engine
         self.n = len(plans)
         self._ph = []
@@ -645,7 +648,7 @@ class Batch:
             self._ph.append(ph)
         arr = (C.c_void_p * self.n)(*[h.value for h in self._ph])
         o = CountOpts(blocks_per_sm, warps_per_block, chunk, time_budget_s, 0, root_stride, root_offset, int(stats),
-                      heavy_threshold, int(not hub_bitmaps))
+                      heavy_threshold, int(not hub_bitmaps), root_max_degree)
         h = C.c_void_p()
         try:
             _check(lib().sge_batch_create(engine._h, arr, self.n, C.byref(o), C.byref(h)))
@@ -709,14 +712,16 @@ def trie_free(t: Trie) -> None:
     lib().sge_trie_free(C.byref(t))
 
 
-def count_host(graph: DataGraph, plans: list[PlanBlob], stats: bool = False):
-    """End-to-end call through sge_count_host: host CSR in, counts out."""
+def count_host(graph: DataGraph, plans: list[PlanBlob], stats: bool = False, root_stride: int = 1,
+               root_offset: int = 0):
+    """End-to-end call through sge_count_host: host CSR in, counts out
+    (root_stride/root_offset: the sampled root edges, as in Engine.count)."""
     arr = (PlanBlob * len(plans))(*plans)
     counts = (u64 * len(plans))()
     st = Stats()
     off = np.ascontiguousarray(graph.offsets, np.uint32)
     nb = np.ascontiguousarray(graph.nbrs, np.uint32)
-    o = CountOpts(0, 0, 0, 0.0, 0, 1, 0, int(stats))
+    o = CountOpts(0, 0, 0, 0.0, 0, root_stride, root_offset, int(stats))
     _check(lib().sge_count_host(_u32p(off), _u32p(nb), graph.num_vertices, nb.size, arr, len(plans), C.byref(o),
                                 counts, C.byref(st)))
     return list(counts), st.as_dict()
