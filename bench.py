@@ -6,10 +6,13 @@ Default workload (the configuration the headline metric is quoted on):
 (PatternGraph.random(7, 16 + i % 4, 2000 + i)) counted on a seeded R-MAT data
 graph with 2^22 vertices and 64M undirected edges (a=.57 b=.19 c=.19, seed 4,
 deduplicated, self-loop-free, ids unpermuted), built on the GPU.  Exact counts
-of these dense patterns over all 64M root edges are beyond any executor (the
-reference needs more than a minute for one of them on a 65K-edge R-MAT), so a
-step counts a fixed root sample: the undirected root edges
-e ≡ SAMPLE_OFFSET (mod SAMPLE_STRIDE) in CSR order, both orientations.  For
+of these dense patterns over all 64M root edges are beyond any executor: the
+reference needs more than a minute for one of them on a 65K-edge R-MAT, 61
+sampled root edges already hold ~1e15 instances of a pattern, and a single
+root between two degree-3,000 vertices holds 1.4e9 (about 3,000 CPU
+core-seconds).  So a step counts a fixed root sample: the undirected root
+edges e ≡ SAMPLE_OFFSET (mod SAMPLE_STRIDE) in CSR order, both orientations,
+whose two endpoints both have degree <= ROOT_MAX_DEGREE.  For
 each pattern the planner keeps one symmetry-restriction sequence and one
 root pattern edge (canonical_symmetry), so every plan of a pattern counts
 the same instances on the sample and the two planners below are compared on
@@ -59,9 +62,12 @@ sys.path.insert(0, str(PKG))
 METRIC = "embeddings/sec on 1 GB300, learned+batched vs plain plan, bit-exact; %HBM peak"
 
 RMAT22 = dict(scale=22, m=64_000_000, a=0.57, b=0.19, c=0.19, seed=4)
-SAMPLE_STRIDE = 1 << 20      # root edges e ≡ SAMPLE_OFFSET (mod SAMPLE_STRIDE)
+SAMPLE_STRIDE = 1 << 16      # root edges e ≡ SAMPLE_OFFSET (mod SAMPLE_STRIDE) ...
 SAMPLE_OFFSET = 1
-CPU_SUBSAMPLE = 16           # the CPU runs every CPU_SUBSAMPLE-th edge of the sample
+ROOT_MAX_DEGREE = 1000       # ... whose endpoints both have degree <= ROOT_MAX_DEGREE
+CPU_SUBSAMPLE = 16           # the CPU runs every CPU_SUBSAMPLE-th edge of the sample ...
+CPU_SLICES = 13              # ... for 78/13 = 6 patterns per reference-arm step (a 13-step cycle covers all)
+CPU_CHECK_EVERY = 6          # cpu_baseline and the GPU/CPU check: patterns i ≡ 0 (mod 6), 13 of them
 N_PATTERNS = 78
 
 CL_GRAPH = dict(n=7100, m=100_000, gamma=2.1, max_deg=1000, seed=2)
@@ -211,16 +217,18 @@ def sample_opts(world: int = 1, rank: int = 0, sub: int = 1) -> dict:
     this rank's share).  Edges e ≡ SAMPLE_OFFSET (mod SAMPLE_STRIDE) split as
     e ≡ SAMPLE_OFFSET + j·SAMPLE_STRIDE (mod SAMPLE_STRIDE·n), j < n."""
     n = world * sub
-    return dict(root_stride=SAMPLE_STRIDE * n, root_offset=SAMPLE_OFFSET + rank * SAMPLE_STRIDE)
+    return dict(root_stride=SAMPLE_STRIDE * n, root_offset=SAMPLE_OFFSET + rank * SAMPLE_STRIDE,
+                root_max_degree=ROOT_MAX_DEGREE)
 
 
 def rmat22_config(extra: dict | None = None) -> dict:
     c = {"workload": f"rmat_s22_m64M x 78 random 7-vertex patterns (16-19 edges), root sample: undirected edges "
-                     f"e = {SAMPLE_OFFSET} mod {SAMPLE_STRIDE} (CSR order, both orientations)",
+                     f"e = {SAMPLE_OFFSET} mod {SAMPLE_STRIDE} (CSR order, both orientations) with both endpoint "
+                     f"degrees <= {ROOT_MAX_DEGREE}",
          "graph": dict(RMAT22, generator="rmat", ids="unpermuted", built="on the GPU (sge_graph_create_rmat)"),
          "patterns": "PatternGraph.random(7, 16 + i % 4, 2000 + i), i < 78",
-         "root_sample": {"stride": SAMPLE_STRIDE, "offset": SAMPLE_OFFSET,
-                         "edges": RMAT22["m"] // SAMPLE_STRIDE},
+         "root_sample": {"stride": SAMPLE_STRIDE, "offset": SAMPLE_OFFSET, "max_endpoint_degree": ROOT_MAX_DEGREE,
+                         "edges_before_degree_cap": RMAT22["m"] // SAMPLE_STRIDE},
          "symmetry": "per pattern one restriction sequence and root edge for every plan (canonical_symmetry)",
          "l2": "inputs larger than L2 (512 MB CSR + 4 GB hub bitmaps); 512 MiB L2 flush before each timed step",
          "parallelism": "root-edge sharding across ranks"}
@@ -291,14 +299,17 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
     off, nb = oracle_graph(args.workload)
+    og = oracle.Graph(off, nb)
     setup_s = time.perf_counter() - t0
+    slices = 1
     if args.workload == "rmat22":
         blobs = fixture_plans("rmat22_plain")
-        sub = dict(stride=SAMPLE_STRIDE * CPU_SUBSAMPLE, offset=SAMPLE_OFFSET)
-        names = [f"pattern{i}" for i in range(len(blobs))]
-        sample_desc = (f"undirected root edges e = {SAMPLE_OFFSET} mod {SAMPLE_STRIDE * CPU_SUBSAMPLE} (every "
-                       f"{CPU_SUBSAMPLE}th edge of the GPU's sample) of all 78 patterns per step, the cost model's plans "
-                       "with the same symmetry as the GPU's")
+        sub = dict(stride=SAMPLE_STRIDE * CPU_SUBSAMPLE, offset=SAMPLE_OFFSET, root_max_degree=ROOT_MAX_DEGREE)
+        slices = CPU_SLICES
+        sample_desc = (f"undirected root edges e = {SAMPLE_OFFSET} mod {SAMPLE_STRIDE * CPU_SUBSAMPLE} with endpoint "
+                       f"degrees <= {ROOT_MAX_DEGREE} (every {CPU_SUBSAMPLE}th edge of the GPU's sample); step s runs "
+                       f"patterns i = s mod {CPU_SLICES} (a {CPU_SLICES}-step cycle covers all 78), with the cost "
+                       "model's plans under the same symmetry as the GPU's")
         config = rmat22_config()
     else:
         plans = fixture_plans("chunglu7100_plans")
@@ -313,26 +324,26 @@ def run_reference(args):
             t = []
             for cand in (b, a):
                 s = time.perf_counter()
-                oracle.count_plans(off, nb, bytes(cand), 1, threads=threads, stride=64, offset=0)
+                og.count_plans(bytes(cand), 1, threads=threads, stride=64, offset=0)
                 t.append(time.perf_counter() - s)
             blobs.append(a if t[1] < t[0] else b)
-        names = [str(x) for x in fixture_plans("chunglu7100_names")]
         sub = dict(stride=8, offset=0)
         sample_desc = ("undirected root edges e = 0 mod 8 of all 12 plans per step; IEP modes run the faster on "
                        "the host of the engine's plan and the best inclusion-exclusion plan")
         config = chunglu_config()
-    raw = b"".join(bytes(b) for b in blobs)
     mult = [blob_multiplier(b) for b in blobs]
 
-    def step():
+    def step(j):
+        sel = [i for i in range(len(blobs)) if i % slices == j % slices]
+        raw = b"".join(bytes(blobs[i]) for i in sel)
         s = time.perf_counter()
-        inst, roots = oracle.count_plans(off, nb, raw, len(blobs), threads=threads, **sub)
-        return sum(i * m for i, m in zip(inst, mult)) % (1 << 64), time.perf_counter() - s, sum(roots)
-    for _ in range(args.warmup):
-        step()
+        inst, roots = og.count_plans(raw, len(sel), threads=threads, **sub)
+        return sum(i * mult[k] for i, k in zip(inst, sel)) % (1 << 64), time.perf_counter() - s, sum(roots)
+    for j in range(args.warmup):
+        step(j)
     tot_c, tot_t, tot_r = 0, 0.0, 0
-    for _ in range(args.steps):
-        c, t, r = step()
+    for j in range(args.steps):
+        c, t, r = step(args.warmup + j)
         tot_c += c
         tot_t += t
         tot_r += r
@@ -349,7 +360,7 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------ GPU arm ----
-def cpu_port_check(off, nb, plans, gpu_sub_counts, sub: dict, budget_s: float = 30.0) -> dict:
+def cpu_port_check(off, nb, plans, gpu_sub_counts, sub: dict, what: str = "") -> dict:
     """The oracle port on every host core over a sub-sample of the step's
     roots, with the step's own plans: its rate is the CPU baseline, and its
     counts must equal the GPU's on the same sub-sample."""
@@ -357,14 +368,18 @@ def cpu_port_check(off, nb, plans, gpu_sub_counts, sub: dict, budget_s: float = 
     import oracle
     threads = os.cpu_count() or 1
     raw = b"".join(b.to_bytes() for b in plans)
+    og = oracle.Graph(off, nb)
     t0 = time.perf_counter()
-    inst, roots = oracle.count_plans(off, nb, raw, len(plans), threads=threads, **sub)
+    inst, roots = og.count_plans(raw, len(plans), threads=threads, stride=sub["root_stride"],
+                                 offset=sub["root_offset"], root_max_degree=sub.get("root_max_degree", 0))
     dt = time.perf_counter() - t0
+    og.close()
     cpu = [i * b.count_multiplier % (1 << 64) for i, b in zip(inst, plans)]
+    cap = f" with endpoint degrees <= {sub['root_max_degree']}" if sub.get("root_max_degree") else ""
     return {"value": sum(cpu) / dt, "unit": "embeddings/s", "cores": threads, "kind": "port",
-            "sample": f"undirected root edges e = {sub['root_offset']} mod {sub['root_stride']} of all "
-                      f"{len(plans)} plans ({sum(roots)} root tasks, {dt:.1f} s); value = embeddings of the "
-                      "sample / its time",
+            "sample": f"undirected root edges e = {sub['root_offset']} mod {sub['root_stride']}{cap} of "
+                      f"{what or 'all'} {len(plans)} plans ({sum(roots)} root tasks, {dt:.1f} s); value = embeddings "
+                      "of the sample / its time",
             "parity_with_gpu": cpu == list(gpu_sub_counts), "seconds": dt}
 
 
@@ -495,8 +510,11 @@ def run_rmat22(args):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         sub = sample_opts(1, 0, CPU_SUBSAMPLE)
-        gsub, _, _ = eng.count(plans, **sub)
-        line["cpu_baseline"] = cpu_port_check(eng.graph.offsets, eng.graph.nbrs, plans, gsub, sub)
+        chk = [b for i, b in enumerate(plans) if i % CPU_CHECK_EVERY == 0]
+        gsub, _, gst = eng.count(chk, **sub)
+        line["cpu_baseline"] = cpu_port_check(eng.graph.offsets, eng.graph.nbrs, chk, gsub, sub,
+                                              f"patterns i = 0 mod {CPU_CHECK_EVERY}:")
+        line["cpu_baseline"]["gpu_value_same_sample"] = sum(gsub) / (gst["kernel_ms"] / 1e3)
     eng.close()
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -47,6 +47,12 @@ def lib() -> C.CDLL:
         L.oracle_count_plans.restype = None
         L.oracle_count_plans.argtypes = [_P(u32), _P(u32), u32, C.c_void_p, u32, C.c_int, u64, u64, u32, _P(u64),
                                          _P(u64)]
+        L.oracle_ctx_create.restype = C.c_void_p
+        L.oracle_ctx_create.argtypes = [_P(u32), _P(u32), u32]
+        L.oracle_ctx_free.restype = None
+        L.oracle_ctx_free.argtypes = [C.c_void_p]
+        L.oracle_ctx_count_plans.restype = None
+        L.oracle_ctx_count_plans.argtypes = [C.c_void_p, C.c_void_p, u32, C.c_int, u64, u64, u32, _P(u64), _P(u64)]
         L.oracle_max_threads.restype = C.c_int
         L.oracle_list_embeddings.restype = u64
         L.oracle_list_embeddings.argtypes = [_P(u32), _P(u32), u32, u32, u32, _P(u32), _P(u32), u64]
@@ -144,6 +150,32 @@ def count_plans(offsets, nbrs, blobs: bytes, nplans: int, threads: int = 0, stri
     lib().oracle_count_plans(_p(off), _p(nb), off.size - 1, C.addressof(buf), nplans, threads, stride, offset,
                              root_max_degree, counts, roots)
     return [int(x) for x in counts], [int(x) for x in roots]
+
+
+class Graph:
+    """A CSR prepared once (root edge list) for many counting calls."""
+
+    def __init__(self, offsets, nbrs):
+        self.off, self.nb = _arr(offsets), _arr(nbrs)
+        self._h = lib().oracle_ctx_create(_p(self.off), _p(self.nb), self.off.size - 1)
+
+    def count_plans(self, blobs: bytes, nplans: int, threads: int = 0, stride: int = 1, offset: int = 0,
+                    root_max_degree: int = 0) -> tuple[list[int], list[int]]:
+        """As count_plans(), on this graph."""
+        buf = C.create_string_buffer(bytes(blobs), len(blobs))
+        counts = (u64 * nplans)()
+        roots = (u64 * nplans)()
+        lib().oracle_ctx_count_plans(self._h, C.addressof(buf), nplans, threads, stride, offset, root_max_degree,
+                                     counts, roots)
+        return [int(x) for x in counts], [int(x) for x in roots]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().oracle_ctx_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
 
 
 def max_threads() -> int:

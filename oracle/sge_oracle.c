@@ -503,6 +503,42 @@ void oracle_count_plans(const uint32_t *off, const uint32_t *nb, uint32_t n, con
     free(ev);
 }
 
+/* A graph prepared once for many counting calls: the root edge list and the
+ * largest degree (building them is a pass over every edge). */
+typedef struct {
+    const uint32_t *off, *nb;
+    uint32_t n, maxdeg;
+    uint32_t *eu, *ev;
+    uint64_t m;
+} oracle_ctx;
+
+void *oracle_ctx_create(const uint32_t *off, const uint32_t *nb, uint32_t n) {
+    oracle_ctx *c = (oracle_ctx *)malloc(sizeof(oracle_ctx));
+    c->off = off;
+    c->nb = nb;
+    c->n = n;
+    c->m = root_edges(off, nb, n, &c->eu, &c->ev, &c->maxdeg);
+    return c;
+}
+
+void oracle_ctx_free(void *h) {
+    oracle_ctx *c = (oracle_ctx *)h;
+    if (!c) return;
+    free(c->eu);
+    free(c->ev);
+    free(c);
+}
+
+/* oracle_count_plans on a prepared graph (the arrays it was made from must
+ * still be alive). */
+void oracle_ctx_count_plans(void *h, const sge_plan_blob *plans, uint32_t nplans, int threads, uint64_t stride,
+                            uint64_t offset, uint32_t root_max_degree, uint64_t *counts, uint64_t *roots) {
+    const oracle_ctx *c = (const oracle_ctx *)h;
+    for (uint32_t i = 0; i < nplans; ++i)
+        counts[i] = count_plan_roots(c->off, c->nb, c->maxdeg, c->eu, c->ev, c->m, &plans[i], threads, stride, offset,
+                                     root_max_degree, &roots[i]);
+}
+
 /* Runs plan p over the sampled undirected root edges e ≡ offset (mod stride)
  * (both orientations when the root is unordered), in parallel like
  * parSharedJoin (matching/parallel.cpp:1154-1486), with one refinement: a root

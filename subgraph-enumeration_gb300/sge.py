@@ -713,7 +713,7 @@ def trie_free(t: Trie) -> None:
 
 
 def count_host(graph: DataGraph, plans: list[PlanBlob], stats: bool = False, root_stride: int = 1,
-               root_offset: int = 0):
+               root_offset: int = 0, root_max_degree: int = 0):
     """End-to-end call through sge_count_host: host CSR in, counts out
     (root_stride/root_offset: the sampled root edges, as in Engine.count)."""
     arr = (PlanBlob * len(plans))(*plans)
@@ -721,7 +721,7 @@ def count_host(graph: DataGraph, plans: list[PlanBlob], stats: bool = False, roo
     st = Stats()
     off = np.ascontiguousarray(graph.offsets, np.uint32)
     nb = np.ascontiguousarray(graph.nbrs, np.uint32)
-    o = CountOpts(0, 0, 0, 0.0, 0, root_stride, root_offset, int(stats))
+    o = CountOpts(0, 0, 0, 0.0, 0, root_stride, root_offset, int(stats), 0, 0, root_max_degree)
     _check(lib().sge_count_host(_u32p(off), _u32p(nb), graph.num_vertices, nb.size, arr, len(plans), C.byref(o),
                                 counts, C.byref(st)))
     return list(counts), st.as_dict()
