@@ -395,15 +395,19 @@ def run_rmat22(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     device = local if torch.cuda.is_available() else 0
     torch.cuda.set_device(device)
-    g = RMAT22
+    g = dict(RMAT22)
+    if args.scale != g["scale"]:
+        g.update(scale=args.scale, m=16 << args.scale)
     t0 = time.perf_counter()
     eng = sge.Engine.rmat_device(g["scale"], g["m"], g["a"], g["b"], g["c"], g["seed"], device=device)
     ingest_s = time.perf_counter() - t0
     info = eng.info()
     st = eng.graph.stats()
-    pats = rmat22_patterns(sge)
+    pats = rmat22_patterns(sge)[:args.patterns]
     mlp = sge_learn.load_mlp()
     shard = sample_opts(world, rank)
+    if args.max_level_capacity:
+        shard["max_level_capacity"] = args.max_level_capacity
 
     def barrier():
         if dist:
@@ -476,7 +480,7 @@ def run_rmat22(args):
     for _ in range(max(1, min(args.steps, 2))):
         barrier()
         t = time.perf_counter()
-        ec, _ = sge.count_host(eng.graph, plans, **shard)
+        ec, _ = sge.count_host(eng.graph, plans, **{k: v for k, v in shard.items() if k != "max_level_capacity"})
         e2e_ms.append((time.perf_counter() - t) * 1e3)
         assert ec == counts
     e2e_value = sum(counts) / (statistics.median(e2e_ms) / 1e3)
@@ -489,7 +493,10 @@ def run_rmat22(args):
         "metric": METRIC, "value": value, "unit": "embeddings/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sum_k / len(kernel_ms), "higher_is_better": True,
         "scaling": "strong", "vs_baseline": None, "dtype": "u32 ids / u64 counts", "data": "synthetic",
-        "config": rmat22_config({"ingest_s": ingest_s, "hub_index": {"hubs": info["hub_count"],
+        "config": rmat22_config({"graph": dict(g, generator="rmat", ids="unpermuted",
+                                               built="on the GPU (sge_graph_create_rmat)"),
+                                 "patterns_used": len(pats),
+                                 "ingest_s": ingest_s, "hub_index": {"hubs": info["hub_count"],
                                                                       "min_degree": info["hub_min_degree"]},
                                  "max_degree": info["max_degree"]}),
         "learned_batched": {"wall_s": lw, "planning_s": lp, "kernel_ms": lk, "value_wall": total / lw},
@@ -685,6 +692,12 @@ def main():
     ap.add_argument("--workload", default="rmat22", choices=["rmat22", "chunglu7100", "ingest"])
     ap.add_argument("--plans", default="", help="chunglu7100: comma-separated subset, e.g. house/wcoj-u")
     ap.add_argument("--per-plan", action="store_true", help="chunglu7100: time each plan alone")
+    ap.add_argument("--scale", type=int, default=RMAT22["scale"],
+                    help="rmat22: R-MAT scale (edges 16·2^scale below 22); smaller cases for profiling captures")
+    ap.add_argument("--patterns", type=int, default=N_PATTERNS, help="rmat22: the first N of the 78 patterns")
+    ap.add_argument("--max-level-capacity", type=int, default=0,
+                    help="rmat22: per-level list capacity (0 = max degree; smaller values bound device memory "
+                         "for profiling captures; a list past it fails loudly)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -328,7 +328,12 @@ sge_status sge_plan_from_order_text(uint32_t k, uint32_t m, const uint32_t *edge
 /* Check a plan blob for internal consistency (levels, masks, tail validity). */
 sge_status sge_plan_validate(const sge_plan_blob *blob);
 
-/* ---- device graph (replaces the DataGraph/CandidateSpace the join reads) ---- */
+/* ---- device graph (replaces the DataGraph/CandidateSpace the join reads) ----
+ * Every graph handle also builds a hub index in HBM: a neighbour bitmap for
+ * each vertex of degree >= hub_min_degree (sge_graph_info), the smallest
+ * threshold whose bitmaps fit in min(4 GB, 1/16 of free device memory, and
+ * SGE_HUB_INDEX_MB megabytes when that environment variable is set), so that
+ * a membership test in a high-degree vertex's list is one load. */
 sge_status sge_graph_create(const uint32_t *offsets, const uint32_t *nbrs, uint32_t num_vertices,
                             uint64_t num_directed_edges, int device, sge_graph **out);
 sge_status sge_graph_destroy(sge_graph *g);

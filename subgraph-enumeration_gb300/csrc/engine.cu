@@ -30,6 +30,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <thread>
@@ -1887,7 +1888,8 @@ void to_devplan(const sge_plan_blob &b, DevPlan &d) {
 
 // Hub index: one neighbour bitmap per vertex of degree >= hub_min, with
 // hub_min the smallest threshold (at least 16: shorter lists are searched in
-// a few steps) whose bitmaps fit in min(4 GB, 1/16 of free HBM).  HBM is
+// a few steps) whose bitmaps fit in min(4 GB, 1/16 of free HBM, and
+// SGE_HUB_INDEX_MB when that environment variable is set).  HBM is
 // plentiful next to the CSR, and a membership test in a hub's list, the
 // costliest binary search of the join, becomes one load.
 __global__ void hub_bits_kernel(const uint32_t *off, const uint32_t *adj, const uint32_t *hubs, uint32_t nh,
@@ -1910,7 +1912,8 @@ sge_status build_hub_index(sge_graph *g, const uint32_t *off) {
     for (uint32_t v = 0; v < n; ++v) hist[off[v + 1] - off[v]]++;
     size_t free_b = 0, tot_b = 0;
     CUDA_TRY(cudaMemGetInfo(&free_b, &tot_b));
-    const uint64_t budget = std::min<uint64_t>(4ull << 30, free_b / 16);
+    uint64_t budget = std::min<uint64_t>(4ull << 30, free_b / 16);
+    if (const char *env = getenv("SGE_HUB_INDEX_MB")) budget = std::min<uint64_t>(budget, strtoull(env, nullptr, 10) << 20);
     const uint64_t max_hubs = std::min<uint64_t>(budget / (4 * words), 1u << 20);
     uint64_t above = 0;
     uint32_t thr = g->max_deg + 1;

@@ -638,7 +638,7 @@ class Batch:
     def __init__(self, engine: Engine, plans: list[PlanBlob], stats: bool = False, time_budget_s: float = 0.0,
                  blocks_per_sm: int = 0, warps_per_block: int = 0, chunk: int = 0, root_stride: int = 1,
                  root_offset: int = 0, heavy_threshold: int = 0, hub_bitmaps: bool = True,
-                 root_max_degree: int = 0):
+                 root_max_degree: int = 0, max_level_capacity: int = 0):
         self.engine = engine
         self.n = len(plans)
         self._ph = []
@@ -647,8 +647,8 @@ class Batch:
             _check(lib().sge_plan_create(C.byref(b), C.byref(ph)))
             self._ph.append(ph)
         arr = (C.c_void_p * self.n)(*[h.value for h in self._ph])
-        o = CountOpts(blocks_per_sm, warps_per_block, chunk, time_budget_s, 0, root_stride, root_offset, int(stats),
-                      heavy_threshold, int(not hub_bitmaps), root_max_degree)
+        o = CountOpts(blocks_per_sm, warps_per_block, chunk, time_budget_s, max_level_capacity, root_stride,
+                      root_offset, int(stats), heavy_threshold, int(not hub_bitmaps), root_max_degree)
         h = C.c_void_p()
         try:
             _check(lib().sge_batch_create(engine._h, arr, self.n, C.byref(o), C.byref(h)))
