@@ -416,7 +416,7 @@ def run_rmat22(args):
 
     def plain():
         tw = time.perf_counter()
-        counts, plan_s, kern = [], 0.0, 0.0
+        counts, plan_s, kern, pplans = [], 0.0, 0.0, []
         for p in pats:
             a = time.perf_counter()
             b = plain_plan(sge, p, st)
@@ -424,7 +424,8 @@ def run_rmat22(args):
             c, _, s = eng.count([b], **shard)
             kern += s["kernel_ms"]
             counts.append(c[0])
-        return counts, time.perf_counter() - tw, plan_s, kern
+            pplans.append(b)
+        return counts, time.perf_counter() - tw, plan_s, kern, pplans
 
     def learned():
         tw = time.perf_counter()
@@ -439,9 +440,11 @@ def run_rmat22(args):
     barrier()
     plans, cl, lw, lp, lk = learned()
     barrier()
-    cp, pw, pp, pk = plain()
+    cp, pw, pp, pk, pplans = plain()
     barrier()
     assert cp == cl, "plain and learned plans disagree on the sample"
+    # the plain plans in one batched launch (separates the planner's gain from batching)
+    _, _, spb = eng.count(pplans, **shard)
     # timed steps: replays of the learned batch (CUDA graph), L2 flushed before each
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=f"cuda:{device}")
     batch = eng.batch(plans, **shard)
@@ -502,6 +505,7 @@ def run_rmat22(args):
         "learned_batched": {"wall_s": lw, "planning_s": lp, "kernel_ms": lk, "value_wall": total / lw},
         "plain": {"wall_s": pw, "planning_s": pp, "kernel_ms": pk, "value_wall": total / pw,
                   "launches": len(pats)},
+        "plain_plans_batched_kernel_ms": spb["kernel_ms"],
         "speedup_wall": pw / lw, "speedup_kernel": pk / lk,
         "kernel_ms_without_hub_bitmaps": snh["kernel_ms"],
         "total_count": total,
@@ -522,6 +526,10 @@ def run_rmat22(args):
         line["cpu_baseline"] = cpu_port_check(eng.graph.offsets, eng.graph.nbrs, chk, gsub, sub,
                                               f"patterns i = 0 mod {CPU_CHECK_EVERY}:")
         line["cpu_baseline"]["gpu_value_same_sample"] = sum(gsub) / (gst["kernel_ms"] / 1e3)
+        # the GPU on exactly the reference arm's sample (every 16th edge, all
+        # 78 patterns, the plain plans of its fixture)
+        rc, _, rst = eng.count(pplans, **sub)
+        line["reference_arm_sample_gpu_value"] = sum(rc) / (rst["kernel_ms"] / 1e3)
     eng.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
