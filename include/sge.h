@@ -175,6 +175,9 @@ typedef struct sge_count_opts {
                                    hub bitmaps (for comparison runs); 0 = use them */
     uint32_t root_max_degree;   /* 0 = every sampled root; d > 0: only roots whose two endpoints both have
                                    degree <= d (a bounded sub-sample, e.g. for a CPU check) */
+    uint32_t pin_tables;        /* 0 = pin the root's short lists in per-warp shared-memory tables (a bitmap
+                                   when n <= 32768, else 512-slot hashes); 1 = no tables: less shared
+                                   memory per warp, so more warps resident */
 } sge_count_opts;
 
 /* Statistics of one sge_count call (per call, summed over plans).  kernel_ms,
@@ -208,7 +211,7 @@ typedef struct sge_plan sge_plan;
 /* ---- diagnostics ---- */
 /* sizeof of the ABI structs, for binding checks: 0 sge_plan_blob,
  * 1 sge_plan_opts, 2 sge_count_opts, 3 sge_stats, 4 sge_graph_info,
- * 5 sge_graph_stats, 6 sge_trie. */
+ * 5 sge_graph_stats, 6 sge_trie, 7 sge_plan_tuning. */
 size_t sge_struct_size(int which);
 const char *sge_last_error(void);
 const char *sge_version(void);
@@ -359,6 +362,16 @@ sge_status sge_graph_copy_csr(const sge_graph *g, uint32_t *offsets, uint32_t *n
 /* ---- compiled plans ---- */
 sge_status sge_plan_create(const sge_plan_blob *blob, sge_plan **out);
 sge_status sge_plan_destroy(sge_plan *p);
+/* Execution choices of one plan, set by an autotuner from a short sampled run
+ * (sge_tune.py) or left automatic (all zero).  No counterpart in the
+ * reference, whose OpenMP split is fixed at one task per root
+ * (matching/parallel.cpp:1270-1273).  Counts never depend on them. */
+typedef struct sge_plan_tuning {
+    uint32_t heavy_threshold;   /* 0 = automatic; roots whose level-2 bound exceeds it are split */
+    uint32_t level3_parts;      /* 0 = automatic; parts of each level-3 list per split task (1 = none) */
+    uint32_t no_hub_bitmaps;    /* 1: this plan probes adjacency lists by binary search only */
+} sge_plan_tuning;
+sge_status sge_plan_set_tuning(sge_plan *p, const sge_plan_tuning *t);
 
 /* ---- execution (replaces sharedJoin / parSharedJoin) ----
  * Counts nplans patterns over g in one persistent launch (the batch shares

@@ -95,6 +95,7 @@ struct DevPlan {
     uint32_t tail_par;                            // union of the tail levels' parents
     uint32_t choose_wrap;                         // CHOOSE leaves use the reference's wrapping choosec
     uint32_t root_maxdeg;                         // roots with an endpoint of larger degree are skipped (0 = none)
+    uint32_t no_hubs;                             // this plan probes lists by binary search only
 };
 static_assert(sizeof(DevPlan) % 4 == 0, "DevPlan is copied as 32-bit words");
 
@@ -1580,6 +1581,7 @@ __global__ void __launch_bounds__(COUNT_MAX_WARPS * 32, 7) count_kernel(DevGraph
     auto load_plan = [&](uint32_t pi) {
         const DevPlan &Q = plans[pi];
         ntasks = phase == 0 ? Q.ntasks : H.tot[pi];
+        c.g.hub_min = Q.no_hubs ? 0xFFFFFFFFu : g.hub_min;
     };
     if (nplans) load_plan(0);
     while (cur < nplans) {
@@ -1790,6 +1792,7 @@ DevGraph dev_graph(const sge_graph *g, bool hubs) {
 struct sge_plan {
     sge_plan_blob blob;
     DevPlan dp;
+    sge_plan_tuning tune{};
 };
 
 namespace sge {
@@ -2070,7 +2073,8 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
         if (d.k > SGE_MAX_K) return fail(SGE_UNSUPPORTED, "plan %u has k=%u", i, d.k);
     }
     // pinned-list tables: a bitmap over all vertices when it fits in 4 KB, else a 512-slot hash
-    if (g->n <= 32768u) { L.tmode = 1; L.tw = std::max<uint32_t>(32u, ((g->n + 31u) / 32u + 31u) & ~31u); }
+    if (o.pin_tables) { L.tmode = 0; L.tw = 0; }
+    else if (g->n <= 32768u) { L.tmode = 1; L.tw = std::max<uint32_t>(32u, ((g->n + 31u) / 32u + 31u) & ~31u); }
     else { L.tmode = 2; L.tw = 512; }
     L.want_stats = o.collect_counters != 0;
     for (auto &d : L.dps) d.root_maxdeg = o.root_max_degree;
@@ -2123,7 +2127,10 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
     unsigned long long max_tasks = 1;
     const unsigned long long warps = blocks * L.wpb;
     const double mean_deg = g->stats.moments[1] > 0 ? g->stats.moments[2] / g->stats.moments[1] : 1.0;
-    for (auto &d : L.dps) {
+    for (uint32_t pi = 0; pi < nplans; ++pi) {
+        DevPlan &d = L.dps[pi];
+        const sge_plan_tuning &tu = plans[pi]->tune;
+        d.no_hubs = tu.no_hub_bitmaps ? 1u : 0u;
         // deeper plans do more work per level-2 candidate (and far more under
         // a hub), so their tasks hold fewer candidates: 128 at four
         // enumerated levels, a quarter as many per extra level
@@ -2132,11 +2139,14 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
         // level), a task takes one level-2 candidate and a part of its
         // level-3 list: 8 parts at five enumerated levels, 16 deeper
         const bool split3 = d.ne >= 5 || (d.ne == 4 && !d.pair);
-        const uint32_t split_P3 = split3 ? (d.ne >= 6 ? 16u : 8u) : 1u;
+        const uint32_t split_P3 = split3 ? (tu.level3_parts ? std::min(tu.level3_parts, 1024u)
+                                                            : (d.ne >= 6 ? 16u : 8u))
+                                         : 1u;
         const uint32_t split_S = split3 ? 1u : std::max<uint32_t>(128u >> (2 * deep), 2u);
         const double share = (double)d.ntasks * mean_deg / (double)std::max<unsigned long long>(warps, 1);
-        const uint32_t split_H = o.heavy_threshold ? std::max(o.heavy_threshold, 4u * split_S)
-                                                   : (uint32_t)std::min(1e9, std::max(32.0, share / 4.0));
+        const uint32_t thr = tu.heavy_threshold ? tu.heavy_threshold : o.heavy_threshold;
+        const uint32_t split_H = thr ? std::max(thr, 4u * split_S)
+                                     : (uint32_t)std::min(1e9, std::max(32.0, share / 4.0));
         if (d.ne >= 3 && g->max_deg > split_H) {
             d.split_S = split_S;
             d.split_H = split_H;
@@ -2410,6 +2420,13 @@ sge_status sge_plan_create(const sge_plan_blob *blob, sge_plan **out) {
 
 sge_status sge_plan_destroy(sge_plan *p) {
     delete p;
+    return SGE_OK;
+}
+
+sge_status sge_plan_set_tuning(sge_plan *p, const sge_plan_tuning *t) {
+    if (!p) return fail(SGE_BAD_INPUT, "sge_plan_set_tuning: null plan");
+    if (t) p->tune = *t;
+    else p->tune = sge_plan_tuning{};
     return SGE_OK;
 }
 

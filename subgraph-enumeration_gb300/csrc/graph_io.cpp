@@ -147,6 +147,7 @@ size_t sge_struct_size(int which) {
         case 4: return sizeof(sge_graph_info);
         case 5: return sizeof(sge_graph_stats);
         case 6: return sizeof(sge_trie);
+        case 7: return sizeof(sge_plan_tuning);
         default: return 0;
     }
 }

@@ -80,7 +80,12 @@ class PlanOpts(C.Structure):
 class CountOpts(C.Structure):
     _fields_ = [("blocks_per_sm", u32), ("warps_per_block", u32), ("chunk", u32), ("time_budget_s", C.c_double),
                 ("max_level_capacity", u32), ("root_stride", u64), ("root_offset", u64), ("collect_counters", u32),
-                ("heavy_threshold", u32), ("no_hub_bitmaps", u32), ("root_max_degree", u32)]
+                ("heavy_threshold", u32), ("no_hub_bitmaps", u32), ("root_max_degree", u32), ("pin_tables", u32)]
+
+
+class PlanTuning(C.Structure):
+    """Per-plan execution choices (sge_plan_set_tuning); zero = automatic."""
+    _fields_ = [("heavy_threshold", u32), ("level3_parts", u32), ("no_hub_bitmaps", u32)]
 
 
 class Stats(C.Structure):
@@ -139,6 +144,7 @@ SIGNATURES = {
     "sge_graph_copy_csr": (C.c_int, [C.c_void_p, _P(u32), _P(u32)]),
     "sge_plan_create": (C.c_int, [_P(PlanBlob), _P(C.c_void_p)]),
     "sge_plan_destroy": (C.c_int, [C.c_void_p]),
+    "sge_plan_set_tuning": (C.c_int, [C.c_void_p, C.c_void_p]),
     "sge_count": (C.c_int, [C.c_void_p, _P(C.c_void_p), u32, _P(CountOpts), _P(u64), _P(u64), _P(Stats)]),
     "sge_count_host": (C.c_int, [_P(u32), _P(u32), u32, u64, _P(PlanBlob), u32, _P(CountOpts), _P(u64), _P(Stats)]),
     "sge_plan_candidates": (C.c_int, [u32, u32, _P(u32), _P(GraphStats), _P(PlanOpts), _P(PlanBlob), u32, _P(u32)]),
@@ -561,7 +567,7 @@ class Engine:
     def count(self, plans: list[PlanBlob], stats: bool = False, time_budget_s: float = 0.0,
               max_level_capacity: int = 0, blocks_per_sm: int = 0, warps_per_block: int = 0, chunk: int = 0,
               root_stride: int = 1, root_offset: int = 0, heavy_threshold: int = 0, hub_bitmaps: bool = True,
-              root_max_degree: int = 0):
+              root_max_degree: int = 0, pin_tables: bool = True, tuning: "list[PlanTuning | None] | None" = None):
         """Counts every plan over the graph in one launch.  Returns (counts,
         instances, stats-dict); counts are the reference's "Number of matches"
         (uint64).  stats=True runs the instrumented kernel (set operations,
@@ -571,19 +577,24 @@ class Engine:
         (0 = auto) splits roots whose level-2 list may exceed it into tasks of
         a second launch.  hub_bitmaps=False probes every adjacency list by
         binary search (comparison runs).  root_max_degree > 0 keeps only the
-        sampled roots whose endpoints both have at most that degree."""
+        sampled roots whose endpoints both have at most that degree.
+        pin_tables=False leaves out the per-warp shared-memory tables; tuning
+        gives each plan its PlanTuning (None = automatic)."""
         handles = []
         try:
-            for b in plans:
+            for i, b in enumerate(plans):
                 ph = C.c_void_p()
                 _check(lib().sge_plan_create(C.byref(b), C.byref(ph)))
                 handles.append(ph)
+                if tuning is not None and tuning[i] is not None:
+                    _check(lib().sge_plan_set_tuning(ph, C.byref(tuning[i])))
             arr = (C.c_void_p * len(handles))(*[h.value for h in handles])
             counts = (u64 * len(plans))()
             inst = (u64 * len(plans))()
             st = Stats()
             o = CountOpts(blocks_per_sm, warps_per_block, chunk, time_budget_s, max_level_capacity, root_stride,
-                          root_offset, int(stats), heavy_threshold, int(not hub_bitmaps), root_max_degree)
+                          root_offset, int(stats), heavy_threshold, int(not hub_bitmaps), root_max_degree,
+                          int(not pin_tables))
             _check(lib().sge_count(self._h, arr, len(plans), C.byref(o), counts, inst, C.byref(st)))
             return list(counts), list(inst), st.as_dict()
         finally:
@@ -638,17 +649,21 @@ class Batch:
     def __init__(self, engine: Engine, plans: list[PlanBlob], stats: bool = False, time_budget_s: float = 0.0,
                  blocks_per_sm: int = 0, warps_per_block: int = 0, chunk: int = 0, root_stride: int = 1,
                  root_offset: int = 0, heavy_threshold: int = 0, hub_bitmaps: bool = True,
-                 root_max_degree: int = 0, max_level_capacity: int = 0):
+                 root_max_degree: int = 0, max_level_capacity: int = 0, pin_tables: bool = True,
+                 tuning: "list[PlanTuning | None] | None" = None):
         self.engine = engine
         self.n = len(plans)
         self._ph = []
-        for b in plans:
+        for i, b in enumerate(plans):
             ph = C.c_void_p()
             _check(lib().sge_plan_create(C.byref(b), C.byref(ph)))
             self._ph.append(ph)
+            if tuning is not None and tuning[i] is not None:
+                _check(lib().sge_plan_set_tuning(ph, C.byref(tuning[i])))
         arr = (C.c_void_p * self.n)(*[h.value for h in self._ph])
         o = CountOpts(blocks_per_sm, warps_per_block, chunk, time_budget_s, max_level_capacity, root_stride,
-                      root_offset, int(stats), heavy_threshold, int(not hub_bitmaps), root_max_degree)
+                      root_offset, int(stats), heavy_threshold, int(not hub_bitmaps), root_max_degree,
+                      int(not pin_tables))
         h = C.c_void_p()
         try:
             _check(lib().sge_batch_create(engine._h, arr, self.n, C.byref(o), C.byref(h)))

@@ -28,7 +28,8 @@ def test_bindings_cover_header(sge):
 
 
 @pytest.mark.parametrize("which,cls", [(0, "PlanBlob"), (1, "PlanOpts"), (2, "CountOpts"), (3, "Stats"),
-                                       (4, "GraphInfo"), (5, "GraphStats"), (6, "Trie")])
+                                       (4, "GraphInfo"), (5, "GraphStats"), (6, "Trie"),
+                                       (7, "PlanTuning")])
 def test_struct_layout(sge, which, cls):
     assert sge.lib().sge_struct_size(which) == C.sizeof(getattr(sge, cls))
 
