@@ -388,6 +388,7 @@ def run_rmat22(args):
     import torch
     import sge
     import sge_learn
+    import sge_tune
     world, rank, local = dist_env()
     dist = None
     if world > 1:
@@ -445,9 +446,14 @@ def run_rmat22(args):
     assert cp == cl, "plain and learned plans disagree on the sample"
     # the plain plans in one batched launch (separates the planner's gain from batching)
     _, _, spb = eng.count(pplans, **shard)
-    # timed steps: replays of the learned batch (CUDA graph), L2 flushed before each
+    # the autotuner: shared-memory tables per launch, heavy-root split and hub
+    # use per plan, from short runs on every 4th edge of the sample
+    tt = time.perf_counter()
+    tuned = sge_tune.tune(eng, plans, {k: v for k, v in shard.items() if k != "max_level_capacity"})
+    tune_s = time.perf_counter() - tt
+    # timed steps: replays of the tuned learned batch (CUDA graph), L2 flushed before each
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=f"cuda:{device}")
-    batch = eng.batch(plans, **shard)
+    batch = eng.batch(plans, pin_tables=tuned.pin_tables, tuning=tuned.plans, **shard)
     for _ in range(args.warmup):
         batch.run()
     kernel_ms, launches, counts = [], 0, None
@@ -463,7 +469,7 @@ def run_rmat22(args):
     batch.close()
     # untimed: algorithmic bytes of one step (instrumented kernel) and the
     # same step without hub bitmaps
-    _, _, sst = eng.count(plans, stats=True, **shard)
+    _, _, sst = eng.count(plans, stats=True, pin_tables=tuned.pin_tables, tuning=tuned.plans, **shard)
     _, _, snh = eng.count(plans, hub_bitmaps=False, **shard)
     if dist:
         tc = torch.tensor([x % (1 << 63) for x in counts], dtype=torch.int64, device=f"cuda:{device}")
@@ -502,7 +508,13 @@ def run_rmat22(args):
                                  "ingest_s": ingest_s, "hub_index": {"hubs": info["hub_count"],
                                                                       "min_degree": info["hub_min_degree"]},
                                  "max_degree": info["max_degree"]}),
-        "learned_batched": {"wall_s": lw, "planning_s": lp, "kernel_ms": lk, "value_wall": total / lw},
+        "learned_batched": {"wall_s": lw, "planning_s": lp, "kernel_ms": lk, "value_wall": total / lw,
+                            "note": "planning + one launch with the automatic settings"},
+        "autotuner": {"tuning_s": tune_s, "tuning_kernel_ms": tuned.tuning_ms, "runs": tuned.runs,
+                      "pin_tables": tuned.pin_tables,
+                      "choices": {str(k): tuned.choice.count(k) for k in sorted(set(tuned.choice))},
+                      "candidates": [list(c) for c in sge_tune.CANDIDATES]},
+        "kernel_ms_untuned": lk,
         "plain": {"wall_s": pw, "planning_s": pp, "kernel_ms": pk, "value_wall": total / pw,
                   "launches": len(pats)},
         "plain_plans_batched_kernel_ms": spb["kernel_ms"],

@@ -168,16 +168,19 @@ typedef struct sge_count_opts {
                                    (mod s), in CSR order (both orientations when a plan's root is unordered) */
     uint64_t root_offset;       /* (root-range sharding across ranks, or sampled runs) */
     uint32_t collect_counters;  /* 1: run the instrumented kernel (set_ops, alg_bytes, partial matches) */
-    uint32_t heavy_threshold;   /* 0 = auto; otherwise roots whose level-2 list may exceed it are split
-                                   into tasks of level-2 candidates (128 at four enumerated levels, a
-                                   quarter as many per extra level) run by a second launch */
+    uint32_t heavy_threshold;   /* 0 = auto (a sixteenth of a warp's share of the launch's level-2
+                                   candidates, at least 32); otherwise roots whose level-2 list may
+                                   exceed it are deferred to a second launch that splits each into tasks
+                                   of one level-2 candidate and a part of its level-3 list (or, where
+                                   level 3 is not enumerated, of up to 128 level-2 candidates) */
     uint32_t no_hub_bitmaps;    /* 1: probe every adjacency list by binary search, ignoring the graph's
                                    hub bitmaps (for comparison runs); 0 = use them */
     uint32_t root_max_degree;   /* 0 = every sampled root; d > 0: only roots whose two endpoints both have
                                    degree <= d (a bounded sub-sample, e.g. for a CPU check) */
-    uint32_t pin_tables;        /* 0 = pin the root's short lists in per-warp shared-memory tables (a bitmap
-                                   when n <= 32768, else 512-slot hashes); 1 = no tables: less shared
-                                   memory per warp, so more warps resident */
+    uint32_t pin_tables;        /* per-warp shared-memory tables for the root's lists: 0 = automatic (a
+                                   bitmap when n <= 32768; none on larger graphs with a hub index, whose
+                                   bitmaps serve the long lists, so more warps stay resident); 1 = none;
+                                   2 = 512-slot hashes of the lists of at most 256 on larger graphs */
 } sge_count_opts;
 
 /* Statistics of one sge_count call (per call, summed over plans).  kernel_ms,
@@ -381,6 +384,12 @@ sge_status sge_plan_set_tuning(sge_plan *p, const sge_plan_tuning *t);
 sge_status sge_count(sge_graph *g, const sge_plan *const *plans, uint32_t nplans,
                      const sge_count_opts *opts, uint64_t *counts, uint64_t *instances,
                      sge_stats *stats);
+/* sge_count plus, per plan, the warp-milliseconds its roots took inside the
+ * batched launch (busy_ms[i]: summed over the warps that ran plan i's roots,
+ * both launch phases); what an autotuner compares.  No counterpart in the
+ * reference. */
+sge_status sge_count_plan_times(sge_graph *g, const sge_plan *const *plans, uint32_t nplans,
+                                const sge_count_opts *opts, uint64_t *counts, double *busy_ms, sge_stats *stats);
 /* A batch prepared once and replayed from a captured CUDA graph: the plans
  * are uploaded and the launch sequence (counter reset, both launch phases,
  * read-back of counts, flags and counters) is captured at creation; each run

@@ -1504,6 +1504,7 @@ struct HeavyBuf {
     uint32_t *ids;             // plan p's list at p * cap
     unsigned long long *pre;   // task-count prefix, parallel to ids
     unsigned long long *tot;   // per plan: phase-1 tasks
+    unsigned long long *ptime; // per plan: warp-nanoseconds spent on its roots (both phases)
     uint32_t cap;
 };
 
@@ -1613,7 +1614,10 @@ __global__ void __launch_bounds__(COUNT_MAX_WARPS * 32, 7) count_kernel(DevGraph
             const unsigned long long local = t0 - pre[h];
             const uint2 e = root_edge(g, P, H.ids[(size_t)cur * H.cap + h]);
             const uint32_t c2 = (uint32_t)(local / P.split_P3), q3 = (uint32_t)(local % P.split_P3);
+            unsigned long long tb = 0;
+            if (lane == 0) tb = globaltimer_ns();
             acc += run_root<STATS>(P, W, c, e.x, e.y, c2 * P.split_S, (c2 + 1) * P.split_S, q3, P.split_P3);
+            if (lane == 0) atomicAdd(H.ptime + cur, globaltimer_ns() - tb);
             continue;
         }
         if (P.ne == 2) {
@@ -1637,7 +1641,12 @@ __global__ void __launch_bounds__(COUNT_MAX_WARPS * 32, 7) count_kernel(DevGraph
                 src = msk ? (uint32_t)(__ffs(msk) - 1) : 0u;
             }
             const uint32_t ku = __shfl_sync(FULL_MASK, u, src), kv = __shfl_sync(FULL_MASK, v, src);
-            if (nk) acc += leaf_roots(P, W, c, nk, ku, kv);
+            if (nk) {
+                unsigned long long tb = 0;
+                if (lane == 0) tb = globaltimer_ns();
+                acc += leaf_roots(P, W, c, nk, ku, kv);
+                if (lane == 0) atomicAdd(H.ptime + cur, globaltimer_ns() - tb);
+            }
             roots += nk;
             continue;
         }
@@ -1654,7 +1663,10 @@ __global__ void __launch_bounds__(COUNT_MAX_WARPS * 32, 7) count_kernel(DevGraph
                     continue;
                 }
             }
+            unsigned long long tb = 0;
+            if (lane == 0) tb = globaltimer_ns();
             acc += run_root<STATS>(P, W, c, e.x, e.y);
+            if (lane == 0) atomicAdd(H.ptime + cur, globaltimer_ns() - tb);
         }
     }
     if (cur < nplans && lane == 0 && acc) atomicAdd(counts + cur, acc);
@@ -2045,7 +2057,7 @@ struct LaunchCfg {
     bool want_stats = false, any_split = false, use_hubs = true;
     unsigned long long deadline = 0;
     size_t off_plans = 0, off_counts = 0, off_queue = 0, off_flags = 0, off_stats = 0, off_hcnt = 0, off_htot = 0,
-           off_hids = 0, off_hpre = 0, bytes_zeroed = 0, bytes = 0;
+           off_hids = 0, off_hpre = 0, off_ptime = 0, bytes_zeroed = 0, bytes = 0;
 };
 
 sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t nplans, const sge_count_opts &o,
@@ -2072,10 +2084,15 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
         L.nvs = std::max(L.nvs, plan_nvs(d));
         if (d.k > SGE_MAX_K) return fail(SGE_UNSUPPORTED, "plan %u has k=%u", i, d.k);
     }
-    // pinned-list tables: a bitmap over all vertices when it fits in 4 KB, else a 512-slot hash
-    if (o.pin_tables) { L.tmode = 0; L.tw = 0; }
+    // pinned-list tables: a bitmap over all vertices when it fits in 4 KB.
+    // Larger graphs pin nothing by default: 512-slot hashes (lists of at most
+    // 256) cost 6 KB of shared memory per warp, and with the hub index the
+    // long lists need no table; the freed shared memory keeps more warps
+    // resident (pin_tables = 2 asks for the hashes anyway).
+    if (o.pin_tables == 1) { L.tmode = 0; L.tw = 0; }
     else if (g->n <= 32768u) { L.tmode = 1; L.tw = std::max<uint32_t>(32u, ((g->n + 31u) / 32u + 31u) & ~31u); }
-    else { L.tmode = 2; L.tw = 512; }
+    else if (o.pin_tables == 2 || !g->d_hub_bits || o.no_hub_bitmaps) { L.tmode = 2; L.tw = 512; }
+    else { L.tmode = 0; L.tw = 0; }
     L.want_stats = o.collect_counters != 0;
     for (auto &d : L.dps) d.root_maxdeg = o.root_max_degree;
     L.use_hubs = o.no_hub_bitmaps == 0;
@@ -2146,7 +2163,7 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
         const double share = (double)d.ntasks * mean_deg / (double)std::max<unsigned long long>(warps, 1);
         const uint32_t thr = tu.heavy_threshold ? tu.heavy_threshold : o.heavy_threshold;
         const uint32_t split_H = thr ? std::max(thr, 4u * split_S)
-                                     : (uint32_t)std::min(1e9, std::max(32.0, share / 4.0));
+                                     : (uint32_t)std::min(1e9, std::max(32.0, share / 16.0));
         if (d.ne >= 3 && g->max_deg > split_H) {
             d.split_S = split_S;
             d.split_H = split_H;
@@ -2168,7 +2185,8 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
     L.off_stats = L.off_flags + 256;
     L.off_hcnt = L.off_stats + 256;
     L.off_htot = L.off_hcnt + ((4 * (size_t)nplans + 255) & ~(size_t)255);
-    L.off_hids = L.off_htot + ((8 * (size_t)nplans + 255) & ~(size_t)255);
+    L.off_ptime = L.off_htot + ((8 * (size_t)nplans + 255) & ~(size_t)255);
+    L.off_hids = L.off_ptime + ((8 * (size_t)nplans + 255) & ~(size_t)255);
     L.bytes_zeroed = L.off_hids;
     L.off_hpre = L.off_hids + (((size_t)L.heavy_cap * nplans * 4 + 255) & ~(size_t)255);
     L.bytes = L.off_hpre + (((size_t)L.heavy_cap * nplans * 8 + 255) & ~(size_t)255);
@@ -2189,7 +2207,8 @@ sge_status enqueue_launch(sge_graph *g, const LaunchCfg &L, unsigned char *B, ui
     DevStats *dstats = reinterpret_cast<DevStats *>(B + L.off_stats);
     HeavyBuf H{reinterpret_cast<uint32_t *>(B + L.off_hcnt), reinterpret_cast<uint32_t *>(B + L.off_hids),
                reinterpret_cast<unsigned long long *>(B + L.off_hpre),
-               reinterpret_cast<unsigned long long *>(B + L.off_htot), L.heavy_cap};
+               reinterpret_cast<unsigned long long *>(B + L.off_htot),
+               reinterpret_cast<unsigned long long *>(B + L.off_ptime), L.heavy_cap};
     launches = 0;
     for (uint32_t phase = 0; phase < (L.any_split ? 2u : 1u); ++phase) {
         if (phase == 1) {
@@ -2430,8 +2449,22 @@ sge_status sge_plan_set_tuning(sge_plan *p, const sge_plan_tuning *t) {
     return SGE_OK;
 }
 
+static sge_status count_impl(sge_graph *g, const sge_plan *const *plans, uint32_t nplans, const sge_count_opts *opts,
+                             uint64_t *counts, uint64_t *instances, sge_stats *stats, double *busy_ms);
+
 sge_status sge_count(sge_graph *g, const sge_plan *const *plans, uint32_t nplans, const sge_count_opts *opts,
                      uint64_t *counts, uint64_t *instances, sge_stats *stats) {
+    return count_impl(g, plans, nplans, opts, counts, instances, stats, nullptr);
+}
+
+sge_status sge_count_plan_times(sge_graph *g, const sge_plan *const *plans, uint32_t nplans,
+                                const sge_count_opts *opts, uint64_t *counts, double *busy_ms, sge_stats *stats) {
+    if (!busy_ms && nplans) return fail(SGE_BAD_INPUT, "sge_count_plan_times: null busy_ms");
+    return count_impl(g, plans, nplans, opts, counts, nullptr, stats, busy_ms);
+}
+
+static sge_status count_impl(sge_graph *g, const sge_plan *const *plans, uint32_t nplans, const sge_count_opts *opts,
+                             uint64_t *counts, uint64_t *instances, sge_stats *stats, double *busy_ms) {
     auto t_start = std::chrono::steady_clock::now();
     if (!g || (!plans && nplans) || (!counts && nplans)) return fail(SGE_BAD_INPUT, "sge_count: null argument");
     if (nplans == 0) return SGE_OK;
@@ -2457,7 +2490,10 @@ sge_status sge_count(sge_graph *g, const sge_plan *const *plans, uint32_t nplans
     CUDA_TRY(cudaMemcpyAsync(hc.data(), B + L.off_counts, 8 * nplans, cudaMemcpyDeviceToHost, g->stream));
     CUDA_TRY(cudaMemcpyAsync(&hflags, B + L.off_flags, 4, cudaMemcpyDeviceToHost, g->stream));
     if (L.want_stats) CUDA_TRY(cudaMemcpyAsync(&hs, B + L.off_stats, sizeof hs, cudaMemcpyDeviceToHost, g->stream));
+    std::vector<unsigned long long> hp(busy_ms ? nplans : 0);
+    if (busy_ms) CUDA_TRY(cudaMemcpyAsync(hp.data(), B + L.off_ptime, 8 * (size_t)nplans, cudaMemcpyDeviceToHost, g->stream));
     CUDA_TRY(cudaStreamSynchronize(g->stream));
+    for (uint32_t i = 0; busy_ms && i < nplans; ++i) busy_ms[i] = (double)hp[i] / 1e6;
     float ms = 0;
     cudaEventElapsedTime(&ms, g->ev0, g->ev1);
     return finish_counts(L, hc.data(), hflags, hs, ms, launches, t_start, plans, counts, instances, stats, o);

@@ -146,6 +146,8 @@ SIGNATURES = {
     "sge_plan_destroy": (C.c_int, [C.c_void_p]),
     "sge_plan_set_tuning": (C.c_int, [C.c_void_p, C.c_void_p]),
     "sge_count": (C.c_int, [C.c_void_p, _P(C.c_void_p), u32, _P(CountOpts), _P(u64), _P(u64), _P(Stats)]),
+    "sge_count_plan_times": (C.c_int, [C.c_void_p, _P(C.c_void_p), u32, _P(CountOpts), _P(u64), _P(C.c_double),
+                                       _P(Stats)]),
     "sge_count_host": (C.c_int, [_P(u32), _P(u32), u32, u64, _P(PlanBlob), u32, _P(CountOpts), _P(u64), _P(Stats)]),
     "sge_plan_candidates": (C.c_int, [u32, u32, _P(u32), _P(GraphStats), _P(PlanOpts), _P(PlanBlob), u32, _P(u32)]),
     "sge_plan_features": (C.c_int, [_P(PlanBlob), _P(GraphStats), _P(C.c_float)]),
@@ -567,7 +569,8 @@ class Engine:
     def count(self, plans: list[PlanBlob], stats: bool = False, time_budget_s: float = 0.0,
               max_level_capacity: int = 0, blocks_per_sm: int = 0, warps_per_block: int = 0, chunk: int = 0,
               root_stride: int = 1, root_offset: int = 0, heavy_threshold: int = 0, hub_bitmaps: bool = True,
-              root_max_degree: int = 0, pin_tables: bool = True, tuning: "list[PlanTuning | None] | None" = None):
+              root_max_degree: int = 0, pin_tables: int = 0, tuning: "list[PlanTuning | None] | None" = None,
+              plan_times: bool = False):
         """Counts every plan over the graph in one launch.  Returns (counts,
         instances, stats-dict); counts are the reference's "Number of matches"
         (uint64).  stats=True runs the instrumented kernel (set operations,
@@ -578,8 +581,11 @@ class Engine:
         a second launch.  hub_bitmaps=False probes every adjacency list by
         binary search (comparison runs).  root_max_degree > 0 keeps only the
         sampled roots whose endpoints both have at most that degree.
-        pin_tables=False leaves out the per-warp shared-memory tables; tuning
-        gives each plan its PlanTuning (None = automatic)."""
+        pin_tables: 0 automatic, 1 no per-warp shared-memory tables, 2 hashed
+        tables on large graphs (sge_count_opts.pin_tables); tuning
+        gives each plan its PlanTuning (None = automatic).  plan_times=True
+        also returns stats["plan_busy_ms"]: per plan, the warp-milliseconds
+        its roots took (sge_count_plan_times; instances are then not read)."""
         handles = []
         try:
             for i, b in enumerate(plans):
@@ -594,7 +600,13 @@ class Engine:
             st = Stats()
             o = CountOpts(blocks_per_sm, warps_per_block, chunk, time_budget_s, max_level_capacity, root_stride,
                           root_offset, int(stats), heavy_threshold, int(not hub_bitmaps), root_max_degree,
-                          int(not pin_tables))
+                          int(pin_tables))
+            if plan_times:
+                busy = (C.c_double * len(plans))()
+                _check(lib().sge_count_plan_times(self._h, arr, len(plans), C.byref(o), counts, busy, C.byref(st)))
+                d = st.as_dict()
+                d["plan_busy_ms"] = list(busy)
+                return list(counts), [], d
             _check(lib().sge_count(self._h, arr, len(plans), C.byref(o), counts, inst, C.byref(st)))
             return list(counts), list(inst), st.as_dict()
         finally:
@@ -649,7 +661,7 @@ class Batch:
     def __init__(self, engine: Engine, plans: list[PlanBlob], stats: bool = False, time_budget_s: float = 0.0,
                  blocks_per_sm: int = 0, warps_per_block: int = 0, chunk: int = 0, root_stride: int = 1,
                  root_offset: int = 0, heavy_threshold: int = 0, hub_bitmaps: bool = True,
-                 root_max_degree: int = 0, max_level_capacity: int = 0, pin_tables: bool = True,
+                 root_max_degree: int = 0, max_level_capacity: int = 0, pin_tables: int = 0,
                  tuning: "list[PlanTuning | None] | None" = None):
         self.engine = engine
         self.n = len(plans)
@@ -663,7 +675,7 @@ class Batch:
         arr = (C.c_void_p * self.n)(*[h.value for h in self._ph])
         o = CountOpts(blocks_per_sm, warps_per_block, chunk, time_budget_s, max_level_capacity, root_stride,
                       root_offset, int(stats), heavy_threshold, int(not hub_bitmaps), root_max_degree,
-                      int(not pin_tables))
+                      int(pin_tables))
         h = C.c_void_p()
         try:
             _check(lib().sge_batch_create(engine._h, arr, self.n, C.byref(o), C.byref(h)))
