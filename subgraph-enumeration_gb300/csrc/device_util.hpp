@@ -32,7 +32,9 @@ sge_status device_exclusive_scan(const uint32_t *in, uint32_t *out, uint64_t n, 
 // d_adj: nnz neighbours; symmetric, lists strictly increasing, no
 // self-loops) as a graph, which takes ownership of both arrays (also on
 // failure).  The root-edge list is built on the device; the planner's
-// statistics are computed on the host from a copy of the CSR.
-sge_status graph_adopt(uint32_t *d_off, uint32_t *d_adj, uint32_t n, uint64_t nnz, int device, sge_graph **out);
+// statistics are computed on the host, from h_off/h_adj when the caller has
+// the CSR in host memory, else from a copy.
+sge_status graph_adopt(uint32_t *d_off, uint32_t *d_adj, uint32_t n, uint64_t nnz, int device, sge_graph **out,
+                       const uint32_t *h_off = nullptr, const uint32_t *h_adj = nullptr);
 
 }  // namespace sge

@@ -1986,31 +1986,44 @@ sge_status ensure_batch(sge_graph *g, size_t bytes) {
     return SGE_OK;
 }
 
-// Host validation: sorted, in range, no self-loops, no duplicates; symmetric
-// (full check with threads).
+// Host validation, before any device is touched: offsets monotone, lists
+// sorted strictly increasing, in range, no self-loops; symmetric.  Symmetry
+// costs one search per pair: every entry w > v of N(v) must find v among
+// the entries of N(w) below w, which maps the upper entries one-to-one onto
+// lower ones, so with equally many upper and lower entries every lower entry
+// is some upper entry's mirror too.
 sge_status validate_csr(const uint32_t *off, const uint32_t *nbrs, uint32_t n, uint64_t nnz) {
     if (off[0] != 0 || off[n] != nnz) return fail(SGE_BAD_INPUT, "offsets[0] must be 0 and offsets[n] = %llu", (unsigned long long)nnz);
-    unsigned nt = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    for (uint32_t v = 0; v < n; ++v)
+        if (off[v + 1] < off[v]) return fail(SGE_BAD_INPUT, "offsets not monotone at vertex %u", v);
+    unsigned nt = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
     std::atomic<int> bad{0};
     std::atomic<uint32_t> bad_v{0};
+    std::atomic<uint64_t> upper{0}, lower{0};
     std::vector<std::thread> th;
     for (unsigned t = 0; t < nt; ++t)
         th.emplace_back([&, t]() {
+            uint64_t up = 0, lo = 0;
             for (uint64_t v = t; v < n && !bad.load(std::memory_order_relaxed); v += nt) {
-                uint32_t a = off[v], b = off[v + 1];
-                if (b < a || b > nnz) { bad = 1; bad_v = (uint32_t)v; return; }
+                const uint32_t a = off[v], b = off[v + 1];
                 for (uint32_t e = a; e < b; ++e) {
-                    uint32_t w = nbrs[e];
+                    const uint32_t w = nbrs[e];
                     if (w >= n || w == v || (e > a && nbrs[e - 1] >= w)) { bad = 2; bad_v = (uint32_t)v; return; }
-                    // symmetry: v must appear in N(w)
-                    const uint32_t *p = nbrs + off[w];
-                    const uint32_t *q = nbrs + off[w + 1];
-                    if (off[w + 1] < off[w] || off[w + 1] > nnz) { bad = 1; bad_v = w; return; }
-                    if (!std::binary_search(p, q, (uint32_t)v)) { bad = 3; bad_v = (uint32_t)v; return; }
+                    if (w < v) { ++lo; continue; }
+                    ++up;
+                    // v must be one of N(w)'s entries below w
+                    if (!std::binary_search(nbrs + off[w], nbrs + off[w + 1], (uint32_t)v)) {
+                        bad = 3;
+                        bad_v = (uint32_t)v;
+                        return;
+                    }
                 }
             }
+            upper += up;
+            lower += lo;
         });
     for (auto &x : th) x.join();
+    if (!bad && upper.load() != lower.load()) { bad = 3; bad_v = 0; }
     if (bad == 1) return fail(SGE_BAD_INPUT, "offsets not monotone at vertex %u", (uint32_t)bad_v);
     if (bad == 2) return fail(SGE_BAD_INPUT, "neighbour list of vertex %u is not strictly increasing, out of range, or has a self-loop", (uint32_t)bad_v);
     if (bad == 3) return fail(SGE_BAD_INPUT, "CSR is not symmetric at vertex %u", (uint32_t)bad_v);
@@ -2279,40 +2292,22 @@ sge_status sge_graph_create(const uint32_t *offsets, const uint32_t *nbrs, uint3
     if (device < 0 || device >= ndev) return fail(SGE_BAD_INPUT, "device %d out of range (%d visible)", device, ndev);
     DeviceGuard restore_device;
     CUDA_TRY(cudaSetDevice(device));
-    sge_graph *g = new sge_graph();
-    g->device = device;
-    g->n = n;
-    g->nnz = nnz;
-    g->m = nnz / 2;
-    cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, device);
-    // root edge list (u<v) and degree moments
-    std::vector<uint2> edges;
-    edges.reserve(g->m);
-    for (uint32_t v = 0; v < n; ++v) {
-        uint32_t d = offsets[v + 1] - offsets[v];
-        g->max_deg = std::max(g->max_deg, d);
-        for (uint32_t e = offsets[v]; e < offsets[v + 1]; ++e)
-            if (nbrs[e] > v) edges.push_back(make_uint2(v, nbrs[e]));
-    }
-    sge_graph_stats_compute(offsets, nbrs, n, &g->stats);
-    auto cleanup = [&](sge_status s) { sge_graph_destroy(g); return s; };
+    // upload the CSR; the root edge list is built on the device and the
+    // planner statistics from the host arrays (graph_adopt)
+    uint32_t *d_off = nullptr, *d_adj = nullptr;
     cudaError_t e;
-    if ((e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking)) != cudaSuccess ||
-        (e = cudaEventCreate(&g->ev0)) != cudaSuccess || (e = cudaEventCreate(&g->ev1)) != cudaSuccess)
-        return cleanup(fail(SGE_CUDA_ERROR, "stream/event creation: %s", cudaGetErrorString(e)));
-    if ((e = cudaMalloc(&g->d_off, sizeof(uint32_t) * ((size_t)n + 1))) != cudaSuccess ||
-        (e = cudaMalloc(&g->d_adj, sizeof(uint32_t) * std::max<uint64_t>(nnz, 1))) != cudaSuccess ||
-        (e = cudaMalloc(&g->d_edges, sizeof(uint2) * std::max<uint64_t>(g->m, 1))) != cudaSuccess)
-        return cleanup(fail(SGE_OOM, "device allocation of the graph failed: %s", cudaGetErrorString(e)));
-    if ((e = cudaMemcpyAsync(g->d_off, offsets, sizeof(uint32_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, g->stream)) != cudaSuccess ||
-        (nnz && (e = cudaMemcpyAsync(g->d_adj, nbrs, sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice, g->stream)) != cudaSuccess) ||
-        (g->m && (e = cudaMemcpyAsync(g->d_edges, edges.data(), sizeof(uint2) * g->m, cudaMemcpyHostToDevice, g->stream)) != cudaSuccess) ||
-        (e = cudaStreamSynchronize(g->stream)) != cudaSuccess)
-        return cleanup(fail(SGE_CUDA_ERROR, "graph upload failed: %s", cudaGetErrorString(e)));
-    sge_status hst = build_hub_index(g, offsets);
-    if (hst != SGE_OK) return cleanup(hst);
-    *out = g;
-    return SGE_OK;
+    if ((e = cudaMalloc(&d_off, sizeof(uint32_t) * ((size_t)n + 1))) != cudaSuccess ||
+        (e = cudaMalloc(&d_adj, sizeof(uint32_t) * std::max<uint64_t>(nnz, 1))) != cudaSuccess) {
+        cudaFree(d_off);
+        return fail(SGE_OOM, "device allocation of the graph failed: %s", cudaGetErrorString(e));
+    }
+    if ((e = cudaMemcpy(d_off, offsets, sizeof(uint32_t) * ((size_t)n + 1), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (nnz && (e = cudaMemcpy(d_adj, nbrs, sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice)) != cudaSuccess)) {
+        cudaFree(d_off);
+        cudaFree(d_adj);
+        return fail(SGE_CUDA_ERROR, "graph upload failed: %s", cudaGetErrorString(e));
+    }
+    return graph_adopt(d_off, d_adj, n, nnz, device, out, offsets, nbrs);
 }
 
 }  // extern "C"
@@ -2337,7 +2332,7 @@ __global__ void root_scatter_kernel(const uint32_t *off, const uint32_t *adj, ui
 }  // namespace
 
 sge_status sge::graph_adopt(uint32_t *d_off, uint32_t *d_adj, uint32_t n, uint64_t nnz, int device,
-                            sge_graph **out) {
+                            sge_graph **out, const uint32_t *h_off, const uint32_t *h_adj) {
     sge_graph *g = new sge_graph();
     g->device = device;
     g->d_off = d_off;
@@ -2372,14 +2367,21 @@ sge_status sge::graph_adopt(uint32_t *d_off, uint32_t *d_adj, uint32_t n, uint64
         cudaFree(pos);
         if (st != SGE_OK) return cleanup(st);
     }
-    // planner statistics from a host copy (the same numbers as a host-built graph)
-    std::vector<uint32_t> off((size_t)n + 1), adj(std::max<uint64_t>(nnz, 1));
-    if ((e = cudaMemcpy(off.data(), d_off, 4 * ((size_t)n + 1), cudaMemcpyDeviceToHost)) != cudaSuccess ||
-        (nnz && (e = cudaMemcpy(adj.data(), d_adj, 4 * nnz, cudaMemcpyDeviceToHost)) != cudaSuccess))
-        return cleanup(fail(SGE_CUDA_ERROR, "graph read-back: %s", cudaGetErrorString(e)));
-    for (uint32_t v = 0; v < n; ++v) g->max_deg = std::max(g->max_deg, off[v + 1] - off[v]);
-    sge_graph_stats_compute(off.data(), adj.data(), n, &g->stats);
-    sge_status hst = build_hub_index(g, off.data());
+    // planner statistics from the host arrays (a copy of the device CSR when
+    // it was built on the device: the same numbers as a host-built graph)
+    std::vector<uint32_t> off, adj;
+    if (!h_off) {
+        off.resize((size_t)n + 1);
+        adj.resize(std::max<uint64_t>(nnz, 1));
+        if ((e = cudaMemcpy(off.data(), d_off, 4 * ((size_t)n + 1), cudaMemcpyDeviceToHost)) != cudaSuccess ||
+            (nnz && (e = cudaMemcpy(adj.data(), d_adj, 4 * nnz, cudaMemcpyDeviceToHost)) != cudaSuccess))
+            return cleanup(fail(SGE_CUDA_ERROR, "graph read-back: %s", cudaGetErrorString(e)));
+        h_off = off.data();
+        h_adj = adj.data();
+    }
+    for (uint32_t v = 0; v < n; ++v) g->max_deg = std::max(g->max_deg, h_off[v + 1] - h_off[v]);
+    sge_graph_stats_compute(h_off, h_adj, n, &g->stats);
+    sge_status hst = build_hub_index(g, h_off);
     if (hst != SGE_OK) return cleanup(hst);
     *out = g;
     return SGE_OK;

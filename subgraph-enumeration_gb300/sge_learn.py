@@ -51,17 +51,22 @@ class Records:
 
 
 def record(engine: "sge.Engine", stats, patterns, shortlist: int = 12, stride: int = 8, pattern_offset: int = 0,
-           time_budget_s: float = 5.0, iep: bool = True, rec: Records | None = None) -> Records:
+           time_budget_s: float = 5.0, iep: bool = True, rec: Records | None = None, candidates_fn=None,
+           sample: dict | None = None) -> Records:
     """Runs the cost model's shortlist of every pattern on every stride-th root
-    (the same roots for all candidates of a pattern) and records kernel times."""
+    (the same roots for all candidates of a pattern) and records kernel times.
+    candidates_fn(p, stats, shortlist) replaces the shortlist (e.g. candidates
+    sharing one symmetry scheme and root edge); sample (Engine.count keyword
+    arguments) replaces the stride sample."""
     rec = rec or Records()
     for pi, p in enumerate(patterns):
-        cands = sge.candidates(p, stats, iep=iep, cap=shortlist)
+        cands = candidates_fn(p, stats, shortlist) if candidates_fn else sge.candidates(p, stats, iep=iep, cap=shortlist)
         off = (pattern_offset + pi) % stride
+        opts = dict(sample) if sample is not None else dict(root_stride=stride, root_offset=off)
         counts = []
         for ci, b in enumerate(cands):
             try:
-                c, _, st = engine.count([b], root_stride=stride, root_offset=off, time_budget_s=time_budget_s)
+                c, _, st = engine.count([b], time_budget_s=time_budget_s, **opts)
                 ms = st["kernel_ms"]
             except sge.SgeError as e:
                 if e.status_name != "TIMEOUT":

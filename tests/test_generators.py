@@ -43,3 +43,16 @@ def test_random_patterns_connected(sge):
                         seen.add(int(w))
                         frontier.append(int(w))
             assert len(seen) == k
+
+
+def test_oracle_generators_build_the_library_graphs(sge, oracle):
+    # the CPU reference arm builds its graphs without the library
+    import numpy as np
+    for args in [(10, 8000, 0.57, 0.19, 0.19, 4), (14, 1 << 18, 0.57, 0.19, 0.19, 4)]:
+        g = sge.gen_rmat(*args)
+        off, nb = oracle.gen_rmat(*args)
+        assert np.array_equal(g.offsets, off) and np.array_equal(g.nbrs, nb)
+    for args in [(380, 915, 2.3, 0, 1), (7100, 100_000, 2.1, 1000, 2)]:
+        g = sge.gen_chung_lu(*args)
+        off, nb = oracle.gen_chung_lu(*args)
+        assert np.array_equal(g.offsets, off) and np.array_equal(g.nbrs, nb)
