@@ -498,6 +498,7 @@ def run_rmat22(args):
     d2h = 8 * len(plans) + 4
     peak, peak_kind = peaks()
     achieved = sst["alg_bytes"] / avg_s / 1e9
+    traffic = profile_traffic("count_kernel_rmat22-sample.md")  # DRAM bytes of one step, measured by ncu
     line = {
         "metric": METRIC, "value": value, "unit": "embeddings/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sum_k / len(kernel_ms), "higher_is_better": True,
@@ -521,11 +522,17 @@ def run_rmat22(args):
         "speedup_wall": pw / lw, "speedup_kernel": pk / lk,
         "kernel_ms_without_hub_bitmaps": snh["kernel_ms"],
         "total_count": total,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "traffic": profile_traffic("count_kernel_rmat22-sample.md"),
+        "roofline": {"bound": "latency", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": traffic,
+                     "dram_gbs": traffic / avg_s / 1e9 if traffic else None,
+                     "dram_frac": traffic / avg_s / 1e9 / peak if traffic else None,
                      "alg_bytes_per_launch": sst["alg_bytes"],
-                     "note": "algorithmic bytes = 4·(base + probed list elements) per set operation + 8 B per CSR "
-                             "offset pair, summed by the instrumented kernel over one step"},
+                     "note": "one step = the batched launch sequence (phase 0, task numbering, phase 1); "
+                             "algorithmic bytes = 4 B per scanned element + per probed list 4 B per probe through "
+                             "a hub bitmap or pinned table, else the list as a merge consumes it (+8 B offsets), "
+                             "summed by the instrumented kernel; traffic = ncu DRAM read+write of the same step "
+                             "(profiles/count_kernel_rmat22-sample.md). The working set stays in L1/L2, so the DFS "
+                             "is bound by dependent-load latency, not HBM bandwidth"},
         "e2e": {"value": e2e_value, "unit": "embeddings/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": statistics.median(e2e_ms)},
         "gpu_launches": launches,

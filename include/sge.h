@@ -168,7 +168,7 @@ typedef struct sge_count_opts {
                                    (mod s), in CSR order (both orientations when a plan's root is unordered) */
     uint64_t root_offset;       /* (root-range sharding across ranks, or sampled runs) */
     uint32_t collect_counters;  /* 1: run the instrumented kernel (set_ops, alg_bytes, partial matches) */
-    uint32_t heavy_threshold;   /* 0 = auto (a sixteenth of a warp's share of the launch's level-2
+    uint32_t heavy_threshold;   /* 0 = auto (a quarter of a warp's share of the launch's level-2
                                    candidates, at least 32); otherwise roots whose level-2 list may
                                    exceed it are deferred to a second launch that splits each into tasks
                                    of one level-2 candidate and a part of its level-3 list (or, where

@@ -121,6 +121,7 @@ struct WarpState {
     uint32_t pmode[3];                    // pinned N(m[0]), N(m[1]), level-2 list: 0 none, 1 bitmap, 2 hash
     uint32_t hcnt[SGE_MAX_K];             // hoisted tail lists (buffer slot = level)
     uint32_t hpin;                        // tail level whose hoisted list is pinned in table 2 (0 = none)
+    unsigned long long t_root;            // globaltimer at the start of the current root (per-plan busy time)
 };
 
 // One tail level's candidate set as the leaf probes it: its lists (a pinned
@@ -222,6 +223,13 @@ __device__ __forceinline__ bool csr_has(const DevGraph &g, uint32_t v, const uin
 // Probe cost of a sorted list of len elements searched by bisection (a table
 // or bitmap probe costs 1).
 __device__ __forceinline__ uint32_t search_cost(uint32_t len) { return 2u + (31u - __clz(len + 1u)); }
+// Algorithmic bytes of probing a list of len elements nprobe times (the
+// instrumented kernel's counters): through a table or hub bitmap each probe
+// reads one word; by bisection the list counts as a merge would consume it,
+// plus its offset pair.
+__device__ __forceinline__ unsigned long long probe_bytes(unsigned long long nprobe, uint32_t len, bool table) {
+    return table ? 4ull * nprobe : 8ull + 4ull * len;
+}
 
 __device__ __forceinline__ unsigned long long binom_exact(unsigned long long n, uint32_t r) {
     if (n < r) return 0ull;
@@ -475,7 +483,10 @@ __device__ __forceinline__ uint32_t setop(const DevPlan &P, const WarpState &W, 
     if (STATS) {
         c.set_ops += 1;
         c.alg_bytes += 4ull * blen;
-        for (uint32_t msk = rest; msk; msk &= msk - 1) c.alg_bytes += 8ull + 4ull * W.llen[__ffs(msk) - 1];
+        for (uint32_t msk = rest; msk; msk &= msk - 1) {
+            const uint32_t j = __ffs(msk) - 1;
+            c.alg_bytes += probe_bytes(blen, W.llen[j], (j < 2 && W.pmode[j]) || W.hs[j] >= 0);
+        }
     }
     uint32_t total = 0;
     for (uint32_t off = 0; off < blen; off += 32) {
@@ -598,11 +609,15 @@ __device__ __forceinline__ bool explore_update(const DevPlan &P, WarpState &W, C
         const uint32_t *prev = version_ptr(P, W, c, pj, i);
         uint32_t plen = version_len(P, W, c, pj, i);
         uint32_t *out = c.buf + (size_t)P.slot[j][i] * c.cap;
-        if (STATS) { c.set_ops += 1; c.alg_bytes += 8ull + 4ull * (plen + W.llen[j]); }
         uint32_t total = 0;
         // scan the running list, probe N(m[j]) (pinned table when present)
         const bool pinned = j < 2 && W.pmode[j];
         const bool scan_prev = pinned || plen <= W.llen[j];
+        if (STATS) {
+            c.set_ops += 1;
+            c.alg_bytes += scan_prev ? 4ull * plen + probe_bytes(plen, W.llen[j], pinned || W.hs[j] >= 0)
+                                     : 8ull + 4ull * (plen + W.llen[j]);
+        }
         const uint32_t *sp = scan_prev ? prev : W.lptr[j];
         const uint32_t sl = scan_prev ? plen : W.llen[j];
         for (uint32_t off = 0; off < sl; off += 32) {
@@ -886,7 +901,6 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
                     const uint32_t len = td_len(D, L, q, lane);
                     const unsigned long long own = td_probe_cost(D, L, W, c.g, q, lane);
                     cost = (unsigned long long)len * (allp - own + 1);
-                    if (STATS) bytes += 4ull * len;
                 }
                 cost = warp_sum_u64(cost);
                 if (cost < best) { best = cost; bq = q; }
@@ -898,6 +912,11 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
             bp = td_ptr(D, L, c.g.adj, bq, lane);
             blen = td_len(D, L, bq, lane);
             trim(bp, blen, td_bounds(D, L, lane));
+            if (STATS) {  // the scanned range, and each other list probed once per element of it
+                bytes += 4ull * blen;
+                for (uint32_t q = 0; q < D.nsrc; ++q)
+                    if (q != bq) bytes += probe_bytes(blen, td_len(D, L, q, lane), td_probe_cost(D, L, W, c.g, q, lane) == 1);
+            }
         }
         L.bptr[lane] = bp;
         uint32_t incl = blen;
@@ -1180,8 +1199,8 @@ __device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32
             if (STATS) {
                 unsigned long long by = 4ull * blen;
                 for (uint32_t q = 0; q < ns; ++q)
-                    if ((int32_t)q != bsrc) by += 8ull + 4ull * S.slen[q];
-                if (xpar && bsrc != -1) by += 8ull + 4ull * xl;
+                    if ((int32_t)q != bsrc) by += probe_bytes(blen, S.slen[q], S.stab[q] >= 0 || S.shub[q] >= 0);
+                if (xpar && bsrc != -1) by += probe_bytes(blen, xl, xl >= c.g.hub_min);
                 pbytes += by;
             }
             Bounds b;
@@ -1614,10 +1633,9 @@ __global__ void __launch_bounds__(COUNT_MAX_WARPS * 32, 7) count_kernel(DevGraph
             const unsigned long long local = t0 - pre[h];
             const uint2 e = root_edge(g, P, H.ids[(size_t)cur * H.cap + h]);
             const uint32_t c2 = (uint32_t)(local / P.split_P3), q3 = (uint32_t)(local % P.split_P3);
-            unsigned long long tb = 0;
-            if (lane == 0) tb = globaltimer_ns();
+            if (lane == 0) W.t_root = globaltimer_ns();
             acc += run_root<STATS>(P, W, c, e.x, e.y, c2 * P.split_S, (c2 + 1) * P.split_S, q3, P.split_P3);
-            if (lane == 0) atomicAdd(H.ptime + cur, globaltimer_ns() - tb);
+            if (lane == 0) atomicAdd(H.ptime + cur, globaltimer_ns() - W.t_root);
             continue;
         }
         if (P.ne == 2) {
@@ -1642,10 +1660,9 @@ __global__ void __launch_bounds__(COUNT_MAX_WARPS * 32, 7) count_kernel(DevGraph
             }
             const uint32_t ku = __shfl_sync(FULL_MASK, u, src), kv = __shfl_sync(FULL_MASK, v, src);
             if (nk) {
-                unsigned long long tb = 0;
-                if (lane == 0) tb = globaltimer_ns();
+                if (lane == 0) W.t_root = globaltimer_ns();
                 acc += leaf_roots(P, W, c, nk, ku, kv);
-                if (lane == 0) atomicAdd(H.ptime + cur, globaltimer_ns() - tb);
+                if (lane == 0) atomicAdd(H.ptime + cur, globaltimer_ns() - W.t_root);
             }
             roots += nk;
             continue;
@@ -1663,10 +1680,9 @@ __global__ void __launch_bounds__(COUNT_MAX_WARPS * 32, 7) count_kernel(DevGraph
                     continue;
                 }
             }
-            unsigned long long tb = 0;
-            if (lane == 0) tb = globaltimer_ns();
+            if (lane == 0) W.t_root = globaltimer_ns();
             acc += run_root<STATS>(P, W, c, e.x, e.y);
-            if (lane == 0) atomicAdd(H.ptime + cur, globaltimer_ns() - tb);
+            if (lane == 0) atomicAdd(H.ptime + cur, globaltimer_ns() - W.t_root);
         }
     }
     if (cur < nplans && lane == 0 && acc) atomicAdd(counts + cur, acc);
@@ -2156,7 +2172,10 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
     // of that share (splitting repeats the root's setup in every task)
     unsigned long long max_tasks = 1;
     const unsigned long long warps = blocks * L.wpb;
-    const double mean_deg = g->stats.moments[1] > 0 ? g->stats.moments[2] / g->stats.moments[1] : 1.0;
+    // mean level-2 bound of a root: the size-biased degree, but never more
+    // than the degree cap of a capped sample
+    double mean_deg = g->stats.moments[1] > 0 ? g->stats.moments[2] / g->stats.moments[1] : 1.0;
+    if (o.root_max_degree) mean_deg = std::min(mean_deg, (double)o.root_max_degree);
     for (uint32_t pi = 0; pi < nplans; ++pi) {
         DevPlan &d = L.dps[pi];
         const sge_plan_tuning &tu = plans[pi]->tune;
@@ -2176,7 +2195,7 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
         const double share = (double)d.ntasks * mean_deg / (double)std::max<unsigned long long>(warps, 1);
         const uint32_t thr = tu.heavy_threshold ? tu.heavy_threshold : o.heavy_threshold;
         const uint32_t split_H = thr ? std::max(thr, 4u * split_S)
-                                     : (uint32_t)std::min(1e9, std::max(32.0, share / 16.0));
+                                     : (uint32_t)std::min(1e9, std::max(32.0, share / 4.0));
         if (d.ne >= 3 && g->max_deg > split_H) {
             d.split_S = split_S;
             d.split_H = split_H;
