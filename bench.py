@@ -30,7 +30,9 @@ pattern here is a multi-bag plan).
 
 Other workloads: --workload chunglu7100 (a seeded Chung-Lu n=7,100 graph,
 house / K5-e / 8-edge near-5-clique in the four modes WCOJ, WCOJ+IEP,
-exploration, exploration+IEP; full counts), --workload ingest.
+exploration, exploration+IEP; full counts), --workload ingest, --workload
+bags (the two 6-vertex patterns of the R-MAT 2^24 configuration through their
+bag relations' tries against the plain DFS leaf, on a down-scaled R-MAT).
 
 Arms:
   --impl sge        (default) the CUDA engine through libsge
@@ -709,6 +711,68 @@ def run_ingest(args):
     print(json.dumps(line), flush=True)
 
 
+# the 6-vertex patterns of the R-MAT 2^24 configuration with a decomposition
+# each in the reference's printed form (global bag last): the own vertex of
+# every other bag is a tail level of the imported plan
+BAG_PATTERNS = {
+    "two_triangles_4cycle": ((6, [(0, 1), (0, 2), (1, 2), (3, 4), (3, 5), (4, 5), (1, 3), (2, 4)]),
+                             "num bags: 5\n1,0,2\n3,1,2\n3,4,2\n3,4,5\n3,4,1,2\n"),
+    "c6_two_chords": ((6, [(0, 1), (1, 2), (2, 3), (3, 4), (4, 5), (0, 5), (0, 3), (1, 4)]),
+                      "num bags: 3\n1,2,3\n4,5,0\n0,1,3,4\n"),
+}
+
+
+def run_bags(args):
+    """The bag-relation join against the DFS leaf: per pattern, the imported
+    decomposition (sge_plan_from_order_text, inclusion-exclusion leaf) counted
+    with its tail levels reading the bags' tries (sge_bags_create +
+    sge_plan_use_bags) and without (intersections of adjacency lists), on an
+    R-MAT with 2^scale vertices and 16·2^scale edges (a=.57 b=.19 c=.19,
+    seed 4).  Both must give the same counts; the relation build (count,
+    enumerate, sort, trie) is timed separately from the counting launches."""
+    import sge
+    scale = args.bag_scale
+    eng = sge.Engine.rmat_device(scale, 16 << scale, seed=4)
+    rows = []
+    opts = dict(root_stride=args.bag_stride, root_offset=0)
+    for name, ((k, edges), text) in BAG_PATTERNS.items():
+        p = sge.PatternGraph.from_edges(k, edges)
+        b, nb = sge.plan_from_reference(p, text, eng, iep=True)
+        t0 = time.perf_counter()
+        try:
+            bags = eng.bags(p, text, max_rows=args.bag_max_rows)
+        except sge.SgeError as e:
+            rows.append({"pattern": name, "bags": nb, "relation": f"not built: {e}"})
+            continue
+        build_s = time.perf_counter() - t0
+        info = bags.info()
+        res = {}
+        for arm, bg in (("dfs", None), ("trie", bags)):
+            for _ in range(args.warmup):
+                c, _, st = eng.count([b], bags=[bg], **opts)
+            ms = []
+            for _ in range(args.steps):
+                c, _, st = eng.count([b], bags=[bg], **opts)
+                ms.append(st["kernel_ms"])
+            res[arm] = (c[0], statistics.median(ms), st.get("bag_levels", [0])[0])
+        assert res["dfs"][0] == res["trie"][0], (name, res)
+        rows.append({"pattern": name, "bags": nb, "count": res["dfs"][0], "trie_levels": res["trie"][2],
+                     "relations": info["relations"], "relation_rows": info["rows"],
+                     "relation_bytes": info["device_bytes"], "relation_build_s": round(build_s, 3),
+                     "dfs_kernel_ms": res["dfs"][1], "trie_kernel_ms": res["trie"][1],
+                     "speedup_kernel": res["dfs"][1] / res["trie"][1] if res["trie"][1] else None,
+                     "speedup_incl_build": res["dfs"][1] / (res["trie"][1] + 1e3 * build_s)})
+        bags.close()
+    eng.close()
+    line = {"metric": "bag-relation trie join vs DFS leaf, kernel ms per count (same counts)",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "data": "synthetic", "dtype": "u32 ids",
+            "config": {"workload": f"rmat_s{scale} bags", "graph": dict(scale=scale, m=16 << scale, a=0.57, b=0.19,
+                                                                       c=0.19, seed=4, generator="rmat"),
+                       "root_stride": args.bag_stride, "leaf": "inclusion-exclusion (-u)"},
+            "rows": rows}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -716,7 +780,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="sge", choices=["sge", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="rmat22", choices=["rmat22", "chunglu7100", "ingest"])
+    ap.add_argument("--workload", default="rmat22", choices=["rmat22", "chunglu7100", "ingest", "bags"])
     ap.add_argument("--plans", default="", help="chunglu7100: comma-separated subset, e.g. house/wcoj-u")
     ap.add_argument("--per-plan", action="store_true", help="chunglu7100: time each plan alone")
     ap.add_argument("--scale", type=int, default=RMAT22["scale"],
@@ -725,6 +789,9 @@ def main():
     ap.add_argument("--max-level-capacity", type=int, default=0,
                     help="rmat22: per-level list capacity (0 = max degree; smaller values bound device memory "
                          "for profiling captures; a list past it fails loudly)")
+    ap.add_argument("--bag-scale", type=int, default=16, help="bags: R-MAT scale (16·2^scale edges)")
+    ap.add_argument("--bag-stride", type=int, default=1, help="bags: root sample stride (1 = every root)")
+    ap.add_argument("--bag-max-rows", type=int, default=4_000_000_000, help="bags: tuples per relation at most")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -732,6 +799,8 @@ def main():
         return run_ingest(args)
     if args.workload == "chunglu7100":
         return run_chunglu(args)
+    if args.workload == "bags":
+        return run_bags(args)
     return run_rmat22(args)
 
 

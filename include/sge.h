@@ -437,6 +437,37 @@ sge_status sge_trie_copy_level(const sge_trie *t, uint32_t level, uint32_t *valu
 sge_status sge_match_set(sge_graph *g, const sge_plan *p, uint32_t k, uint32_t m, const uint32_t *edges,
                          uint32_t *host_out, uint64_t cap_rows, uint64_t *n_rows);
 
+/* ---- the bag-relation join (sharedJoin's trie lookups, matching/join.cpp:812-1200) ----
+ * sge_bags_create materialises, on graph g, the relation of every bag of the
+ * decomposition in plan_text (the text sge_plan_from_order_text reads) that
+ * has exactly one attribute of its own and 3 or 4 attributes: all embeddings
+ * of the bag's sub-pattern (nodeJoin, join.cpp:309-421), sorted into a trie
+ * (buildTrie, join.cpp:1713-1717) keyed by the bag's other attributes in
+ * ascending vertex order, the bag's own attribute last.  The first key level
+ * is indexed by vertex id.  Other bags are skipped, and so is a bag whose
+ * relation holds more than max_rows tuples (0 = no limit; 2^32 - 1 at most):
+ * its tail level keeps intersecting adjacency lists.
+ *
+ * sge_plan_use_bags makes up to two tail levels of a WCOJ plan read their
+ * candidate list from a relation: the level of a bag's own vertex, when every
+ * key of the bag is an enumerated level.  Each leaf candidate then looks its
+ * key tuple up once (one dense step, one binary search per further key) and
+ * counts or probes that range in place of intersecting the vertex's
+ * adjacency lists.  The counts do not change.  *levels (may be NULL)
+ * receives the number of such levels; b = NULL detaches.  The bags must
+ * outlive every count and batch that uses the plan, on the graph they were
+ * built on (another graph returns SGE_BAD_INPUT). */
+typedef struct sge_bags sge_bags;
+sge_status sge_bags_create(sge_graph *g, uint32_t k, uint32_t m, const uint32_t *edges, const char *plan_text,
+                           uint64_t max_rows, sge_bags **out);
+/* Relations built, their total tuples and device bytes, and the bags skipped
+ * for max_rows; own_vertices (may be NULL, one entry per relation) receives
+ * each relation's own pattern vertex.  Every output may be NULL. */
+sge_status sge_bags_info(const sge_bags *b, uint32_t *num_relations, uint64_t *rows, uint64_t *device_bytes,
+                         uint32_t *own_vertices, uint32_t *num_skipped);
+sge_status sge_bags_destroy(sge_bags *b);
+sge_status sge_plan_use_bags(sge_plan *p, const sge_bags *b, uint32_t *levels);
+
 /* End-to-end convenience: host CSR in, counts out (H2D copy, count, D2H read
  * and release all inside the call). */
 sge_status sge_count_host(const uint32_t *offsets, const uint32_t *nbrs, uint32_t num_vertices,

@@ -4,6 +4,7 @@
 #include <cstdio>
 #include <cstdarg>
 #include <string>
+#include <vector>
 #include "sge.h"
 
 namespace sge {
@@ -14,6 +15,13 @@ const char *last_error();
 
 // Returns `st` after recording a formatted message.
 sge_status fail(sge_status st, const char *fmt, ...);
+
+// Bags of a decomposition printed by the reference (HyperTree::writeToStream:
+// "num bags: N", then one comma-separated attribute order per bag, the global
+// bag last; or an order file): each bag's attributes in its order.  Checks
+// that every attribute is a vertex of the k-vertex pattern, named once per
+// bag, and that the bags cover every vertex.
+sge_status parse_bag_text(uint32_t k, const char *text, std::vector<std::vector<uint32_t>> &bags);
 
 // splitmix64: the deterministic counter-based generator behind every seeded
 // generator and sampler in the library (same stream on every host).

@@ -63,6 +63,42 @@ struct DevGraph {
     uint32_t hub_words, hub_min;
 };
 
+// A bag relation's trie on the device (sge_trie levels): key columns
+// 0..nkeys-1, the bag's own attribute in column nkeys.  The first key level
+// is dense over vertex ids: [first[v], first[v+1]) are the level-1 nodes
+// under key v (empty when v heads no tuple).  Below it, node p of level l
+// owns children [child[l][p], child[l][p+1]) of level l+1; val[l] are the
+// values of level l (val[0] and child[0] are unused).
+struct DevTrie {
+    const unsigned long long *first;
+    const uint32_t *val[4];
+    const unsigned long long *child[3];
+    uint32_t nkeys, pad_;
+};
+
+// Range [off, off+len) of val[nkeys] under the key tuple key[0..nkeys-1]
+// (len = 0 when the tuple is absent): one dense step, then one binary search
+// per further key within its parent's children.
+__device__ __forceinline__ void trie_range(const DevTrie &T, const uint32_t *key, uint32_t &off, uint32_t &len) {
+    unsigned long long lo = __ldg(T.first + key[0]), hi = __ldg(T.first + key[0] + 1);
+    for (uint32_t c = 1; c < T.nkeys && lo < hi; ++c) {
+        const uint32_t *v = T.val[c] + lo;
+        const uint32_t n = (uint32_t)(hi - lo);
+        uint32_t a = 0, w = n;
+        while (w > 0) {
+            const uint32_t half = w >> 1;
+            if (__ldg(v + a + half) < key[c]) { a += half + 1; w -= half + 1; }
+            else w = half;
+        }
+        if (a == n || __ldg(v + a) != key[c]) { lo = hi; break; }
+        const unsigned long long p = lo + a;
+        lo = __ldg(T.child[c] + p);
+        hi = __ldg(T.child[c] + p + 1);
+    }
+    off = (uint32_t)lo;
+    len = (uint32_t)(hi - lo);
+}
+
 // Compact device form of sge_plan_blob (+ batch bookkeeping).
 struct DevPlan {
     // level masks fit 16 bits (k <= SGE_MAX_K = 16); small fields are bytes,
@@ -96,6 +132,13 @@ struct DevPlan {
     uint32_t choose_wrap;                         // CHOOSE leaves use the reference's wrapping choosec
     uint32_t root_maxdeg;                         // roots with an endpoint of larger degree are skipped (0 = none)
     uint32_t no_hubs;                             // this plan probes lists by binary search only
+    // bag relations (sge_plan_use_bags): up to 2 tail levels read their
+    // candidates from a trie; tri[i] = slot 0/1 of tail level i, -1 = none
+    const DevTrie *tries;                         // the bag set's device array
+    int8_t tri[SGE_MAX_K];
+    uint8_t trel[2];                              // relation of slot j in `tries`
+    uint8_t tkey[2][3];                           // key levels of slot j, in the trie's key order
+    uint8_t ntrie, pad2_[3];
 };
 static_assert(sizeof(DevPlan) % 4 == 0, "DevPlan is copied as 32-bit words");
 
@@ -142,11 +185,18 @@ struct TailDesc {
 // level, each with its own matched values for the levels from L0 on.
 struct LeafState {
     uint32_t cm[32][2];
-    uint32_t coff[32][2];  // CSR offset of each candidate's own lists (slot 0/1)
-    uint32_t clen[32][2];
     const uint32_t *bptr[32];
     uint32_t pref[32];
+    // per slot s and candidate l: (offset, length) of a per-candidate list.
+    // Slots 0/1: the CSR lists of the candidate's own levels; slots 2/3: its
+    // ranges of the bag-relation tries.  Slots 2/3 are last so that a warp's
+    // shared memory holds them only in launches whose plans use tries.
+    uint2 ol[4][32];
 };
+// Shared-memory bytes of a warp's LeafState with ntr trie slots (0..2).
+__host__ __device__ constexpr size_t leaf_bytes(uint32_t ntr) {
+    return sizeof(LeafState) - (2u - ntr) * 32u * sizeof(uint2);
+}
 
 // Pair step (shared memory): level a = ne-2 of the DFS is processed 32
 // candidates x at a time; level a+1's candidates y of all 32 are generated in
@@ -714,7 +764,7 @@ __device__ __forceinline__ void for_tail_lists(const DevPlan &P, const WarpState
     }
     for (uint32_t msk = cand; msk; msk &= msk - 1) {
         const uint32_t j = __ffs(msk) - 1;
-        if (!f(c.g.adj + L.coff[l][j - lc.L0], L.clen[l][j - lc.L0], (int)j, false)) return;
+        if (!f(c.g.adj + L.ol[j - lc.L0][l].x, L.ol[j - lc.L0][l].y, (int)j, false)) return;
     }
 }
 
@@ -734,12 +784,36 @@ __device__ __forceinline__ Bounds td_bounds(const TailDesc &D, const LeafState &
     return b;
 }
 
-__device__ __forceinline__ const uint32_t *td_ptr(const TailDesc &D, const LeafState &L, const uint32_t *adj,
-                                                  uint32_t q, uint32_t l) {
-    return D.kind[q] >= 4 ? adj + L.coff[l][D.kind[q] - 4] : D.ptr[q];
+// Bag relations: candidate l's key tuple selects its range of each trie's
+// last level (the tail level's whole candidate list), stored in slot 2 + j.
+// Returns the lookups' algorithmic bytes: the dense pair of offsets, then
+// one probe word and one offset pair per further key.  (Inlined: a call
+// would make every leaf save its live registers around it.)
+__device__ __forceinline__ unsigned long long trie_lookups(const DevPlan &P, const WarpState &W, LeafState &L,
+                                                        uint32_t L0, uint32_t l) {
+    unsigned long long bytes = 0;
+    for (uint32_t j = 0; j < P.ntrie; ++j) {
+        const DevTrie &Tr = P.tries[P.trel[j]];
+        uint32_t key[3];
+        for (uint32_t q = 0; q < Tr.nkeys; ++q) {
+            const uint32_t lv = P.tkey[j][q];
+            key[q] = lv < L0 ? W.m[lv] : L.cm[l][lv - L0];
+        }
+        trie_range(Tr, key, L.ol[2 + j][l].x, L.ol[2 + j][l].y);
+        bytes += 16ull + 20ull * (Tr.nkeys - 1u);
+    }
+    return bytes;
+}
+
+// Kinds 4..7 are per-candidate lists: slot k-4 of LeafState.ol, relative to
+// D.ptr (the CSR neighbour array for slots 0/1, a trie's last level for 2/3).
+__device__ __forceinline__ const uint32_t *td_ptr(const TailDesc &D, const LeafState &L, uint32_t q, uint32_t l) {
+    const uint32_t k = D.kind[q];
+    return k >= 4 ? D.ptr[q] + L.ol[k - 4][l].x : D.ptr[q];
 }
 __device__ __forceinline__ uint32_t td_len(const TailDesc &D, const LeafState &L, uint32_t q, uint32_t l) {
-    return D.kind[q] >= 4 ? L.clen[l][D.kind[q] - 4] : D.len[q];
+    const uint32_t k = D.kind[q];
+    return k >= 4 ? L.ol[k - 4][l].y : D.len[q];
 }
 
 // y ∈ list q of the level for candidate l.
@@ -752,7 +826,10 @@ __device__ __forceinline__ bool td_has(const TailDesc &D, const LeafState &L, co
         const int32_t hs = D.lvl[q] >= 0 ? W.hs[D.lvl[q]] : -1;
         return hs >= 0 ? hub_has(c.g, hs, y) : contains(D.ptr[q], D.len[q], y);
     }
-    return csr_has(c.g, L.cm[l][k - 4], c.g.adj + L.coff[l][k - 4], L.clen[l][k - 4], y);
+    const uint32_t sl = k - 4;
+    const uint2 r = L.ol[sl][l];
+    const int32_t hs = sl < 2 ? hub_slot_of(c.g, L.cm[l][sl], r.y) : -1;  // (a trie range has no bitmap)
+    return hs >= 0 ? hub_has(c.g, hs, y) : contains(D.ptr[q] + r.x, r.y, y);
 }
 
 // Cost of probing list q for candidate l (1: pinned table or hub bitmap).
@@ -761,8 +838,8 @@ __device__ __forceinline__ uint32_t td_probe_cost(const TailDesc &D, const LeafS
     const uint32_t k = D.kind[q];
     if (k < 3) return 1u;
     if (k == 3) return (D.lvl[q] >= 0 && W.hs[D.lvl[q]] >= 0) ? 1u : search_cost(D.len[q]);
-    const uint32_t len = L.clen[l][k - 4];
-    return len >= g.hub_min ? 1u : search_cost(len);
+    const uint32_t len = L.ol[k - 4][l].y;
+    return (k < 6 && len >= g.hub_min) ? 1u : search_cost(len);
 }
 
 __device__ __forceinline__ bool td_excluded(const TailDesc &D, const LeafState &L, uint32_t l, uint32_t y) {
@@ -789,13 +866,24 @@ template <bool STATS>
 __device__ void tail_desc(const DevPlan &P, const WarpState &W, const LeafState &L, const Ctx<STATS> &c,
                           const LeafCtx &lc, uint32_t i, TailDesc &D) {
     uint32_t n = 0;
+    if (P.ntrie && P.tri[i] >= 0) {
+        // the bag relation's trie: each candidate's child range (looked up at
+        // the start of the leaf) is the whole candidate list
+        const uint32_t j = (uint32_t)P.tri[i];
+        const DevTrie &T = P.tries[P.trel[j]];
+        D.kind[0] = (uint8_t)(6 + j);
+        D.lvl[0] = -1;
+        D.ptr[0] = T.val[T.nkeys];
+        D.len[0] = 0;
+        n = 1;
+    } else
     for_tail_lists(P, W, L, c, lc, 0, i, [&](const uint32_t *p, uint32_t len, int src, bool pinned) {
         uint32_t k = 3;
         if (pinned) k = (src == SRC_LEVEL2_LIST || src == SRC_HOISTED) ? 2u : (uint32_t)src;
         else if (src >= (int)lc.L0 && src < SRC_LEVEL2_LIST) k = 4u + (uint32_t)src - lc.L0;
         D.kind[n] = (uint8_t)k;
         D.lvl[n] = (int8_t)((k == 3 && src >= 0 && src < (int)lc.L0) ? src : -1);
-        D.ptr[n] = p;
+        D.ptr[n] = k >= 4 ? c.g.adj : p;
         D.len[n] = len;
         ++n;
         return true;
@@ -838,6 +926,8 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
     // lane t describes tail level ne+t (IEP passes probe the later levels too)
     __syncwarp();
     if (lane < passes) tail_desc(P, W, L, c, lc, ne + lane, c.td[lane]);
+    unsigned long long tbytes = 0;
+    if (P.ntrie && lane < ncand) tbytes = trie_lookups(P, W, L, L0, lane);
     if (P.tail_mode != SGE_TAIL_SINGLE) {
         for (uint32_t q = 0; q < c.cs; ++q) c.cnt[lane * c.cs + q] = 0;
     }
@@ -855,7 +945,7 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
         for (uint32_t q = 0; q < passes; ++q)
             if (c.td[q].nsrc == 1) ord |= q << (4 * n++);
     }
-    unsigned long long single = 0, bytes = 0;
+    unsigned long long single = 0, bytes = tbytes;
     for (uint32_t t = 0; t < passes; ++t) {
         const uint32_t tp = (ord >> (4 * t)) & 15u;
         const TailDesc &D = c.td[tp];
@@ -866,7 +956,7 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
         const bool direct = (P.tail_mode != SGE_TAIL_IEP || t + 1 == T) && D.nsrc == 1;
         if (direct) {
             if (lane < ncand) {
-                const uint32_t *fp = td_ptr(D, L, c.g.adj, 0, lane);
+                const uint32_t *fp = td_ptr(D, L, 0, lane);
                 const uint32_t fl = td_len(D, L, 0, lane);
                 const Bounds b = td_bounds(D, L, lane);
                 const uint32_t *bp = fp;
@@ -909,7 +999,7 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
         const uint32_t *bp = nullptr;
         uint32_t blen = 0;
         if (lane < ncand) {
-            bp = td_ptr(D, L, c.g.adj, bq, lane);
+            bp = td_ptr(D, L, bq, lane);
             blen = td_len(D, L, bq, lane);
             trim(bp, blen, td_bounds(D, L, lane));
             if (STATS) {  // the scanned range, and each other list probed once per element of it
@@ -1014,8 +1104,8 @@ __device__ unsigned long long leaf_roots(const DevPlan &P, WarpState &W, Ctx<STA
     if (lane < n) {
         L.cm[lane][0] = u;
         L.cm[lane][1] = v;
-        nbr_off(c.g, u, L.coff[lane][0], L.clen[lane][0]);
-        nbr_off(c.g, v, L.coff[lane][1], L.clen[lane][1]);
+        nbr_off(c.g, u, L.ol[0][lane].x, L.ol[0][lane].y);
+        nbr_off(c.g, v, L.ol[1][lane].x, L.ol[1][lane].y);
     }
     __syncwarp();
     return leaf_chunk(P, W, c, 0, n);
@@ -1033,8 +1123,8 @@ __device__ __forceinline__ unsigned long long pair_flush(const DevPlan &P, WarpS
         const uint32_t x = S.qx[lane], y = S.qy[lane];
         L.cm[lane][0] = x;
         L.cm[lane][1] = y;
-        if ((P.tail_par >> a) & 1u) nbr_off(c.g, x, L.coff[lane][0], L.clen[lane][0]);
-        if ((P.tail_par >> (a + 1)) & 1u) nbr_off(c.g, y, L.coff[lane][1], L.clen[lane][1]);
+        if ((P.tail_par >> a) & 1u) nbr_off(c.g, x, L.ol[0][lane].x, L.ol[0][lane].y);
+        if ((P.tail_par >> (a + 1)) & 1u) nbr_off(c.g, y, L.ol[1][lane].x, L.ol[1][lane].y);
     }
     __syncwarp();
     return leaf_chunk(P, W, c, a, nq);
@@ -1393,7 +1483,7 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
                 if (valid) {
                     const uint32_t rk = __popc(bal & ((1u << lane) - 1u));
                     L.cm[rk][0] = x;
-                    if ((P.tail_par >> L0) & 1u) nbr_off(c.g, x, L.coff[rk][0], L.clen[rk][0]);
+                    if ((P.tail_par >> L0) & 1u) nbr_off(c.g, x, L.ol[0][rk].x, L.ol[0][rk].y);
                 }
                 __syncwarp();
                 if (nc) acc += leaf_chunk(P, W, c, L0, nc);
@@ -1442,20 +1532,22 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
 // plans themselves stay in global memory (read through L1): the fewer bytes a
 // warp holds, the more warps are resident, and the DFS is latency-bound.
 __host__ __device__ constexpr size_t align128(size_t x) { return (x + 127) & ~(size_t)127; }
-__host__ __device__ inline size_t warp_smem_bytes(uint32_t tw, uint32_t ntd, uint32_t cs, uint32_t nvs) {
-    return align128(sizeof(WarpState)) + align128(sizeof(LeafState)) + align128(sizeof(PairState)) +
+__host__ __device__ inline size_t warp_smem_bytes(uint32_t tw, uint32_t ntd, uint32_t cs, uint32_t nvs,
+                                                  uint32_t ntr = 0) {
+    return align128(sizeof(WarpState)) + align128(leaf_bytes(ntr)) + align128(sizeof(PairState)) +
            align128(ntd * sizeof(TailDesc)) + align128(32ull * cs * sizeof(uint32_t)) +
            align128(nvs * sizeof(uint32_t)) + align128(3ull * tw * sizeof(uint32_t));
 }
 
 template <bool STATS>
 __device__ __forceinline__ WarpState &setup_warp(unsigned char *smem, uint32_t wib, uint32_t tw, uint32_t tmode,
-                                                 uint32_t ntd, uint32_t cs, uint32_t nvs, Ctx<STATS> &c) {
-    unsigned char *base = smem + (size_t)wib * warp_smem_bytes(tw, ntd, cs, nvs);
+                                                 uint32_t ntd, uint32_t cs, uint32_t nvs, Ctx<STATS> &c,
+                                                 uint32_t ntr = 0) {
+    unsigned char *base = smem + (size_t)wib * warp_smem_bytes(tw, ntd, cs, nvs, ntr);
     WarpState &W = *reinterpret_cast<WarpState *>(base);
     base += align128(sizeof(WarpState));
     c.L = reinterpret_cast<LeafState *>(base);
-    base += align128(sizeof(LeafState));
+    base += align128(leaf_bytes(ntr));
     c.PS = reinterpret_cast<PairState *>(base);
     base += align128(sizeof(PairState));
     c.td = reinterpret_cast<TailDesc *>(base);
@@ -1570,7 +1662,7 @@ __global__ void __launch_bounds__(COUNT_MAX_WARPS * 32, 7) count_kernel(DevGraph
                                                     uint32_t *scratch, uint32_t cap, uint32_t bufs_per_warp,
                                                     uint32_t tw, uint32_t tmode, unsigned long long deadline_ns,
                                                     uint32_t *flags, DevStats *stats, uint32_t phase, HeavyBuf H,
-                                                    uint32_t ntd, uint32_t cs, uint32_t nvs) {
+                                                    uint32_t ntd, uint32_t cs, uint32_t nvs, uint32_t ntr) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t lane = lane_id();
     const uint32_t wib = threadIdx.x >> 5;
@@ -1581,7 +1673,7 @@ __global__ void __launch_bounds__(COUNT_MAX_WARPS * 32, 7) count_kernel(DevGraph
     c.cap = cap;
     c.flags = flags;
     c.set_ops = c.alg_bytes = c.partial = 0;
-    WarpState &W = setup_warp(smem_raw, wib, tw, tmode, ntd, cs, nvs, c);
+    WarpState &W = setup_warp(smem_raw, wib, tw, tmode, ntd, cs, nvs, c, ntr);
     unsigned long long roots = 0;
     // The time budget covers both launch phases: phase 0's first block
     // records its start next to the flags, and phase 1 measures from there.
@@ -1817,10 +1909,34 @@ DevGraph dev_graph(const sge_graph *g, bool hubs) {
 }
 }  // namespace
 
+// Bag relations of a decomposition on one graph (sge_bags_create): for each
+// bag with exactly one attribute of its own, the bag's tuples (the
+// reference's nodeJoin, matching/join.cpp:309-421) as a trie
+// (buildTrie, join.cpp:1713-1717) whose key columns are the bag's other
+// attributes in ascending vertex order and whose last column is its own one.
+struct BagRel {
+    uint32_t priv = 0;                    // the bag's own pattern vertex
+    uint32_t nkeys = 0;
+    uint32_t keys[3] = {};                // its other attributes, ascending
+    uint64_t rows = 0;
+    sge_trie trie{};
+    unsigned long long *first = nullptr;  // dense first key level (n + 1 offsets)
+};
+struct sge_bags {
+    const sge_graph *g = nullptr;
+    int device = 0;
+    uint32_t k = 0;
+    std::vector<BagRel> rels;
+    DevTrie *d_tries = nullptr;
+    uint64_t bytes = 0;
+    uint32_t skipped = 0;  // bags whose relation exceeded max_rows
+};
+
 struct sge_plan {
     sge_plan_blob blob;
     DevPlan dp;
     sge_plan_tuning tune{};
+    const sge_bags *bags = nullptr;  // bag relations its tail levels read (sge_plan_use_bags)
 };
 
 namespace sge {
@@ -2082,6 +2198,7 @@ struct LaunchCfg {
     std::vector<DevPlan> dps;
     uint32_t nplans = 0, wpb = 8, threads = 256, tmode = 0, tw = 0, cap = 0, nbufs = 1, heavy_cap = 1;
     uint32_t ntd = 1, cs = 1, nvs = 1;  // per-warp tail descriptors, leaf counters, version slots (largest plan)
+    uint32_t ntr = 0;                   // per-warp trie ranges (bag relations of the plans)
     size_t smem = 0, blocks = 1, scratch_bytes = 0;
     bool want_stats = false, any_split = false, use_hubs = true;
     unsigned long long deadline = 0;
@@ -2111,6 +2228,9 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
         L.ntd = std::max(L.ntd, plan_ntd(d));
         L.cs = std::max(L.cs, plan_cs(d));
         L.nvs = std::max(L.nvs, plan_nvs(d));
+        L.ntr = std::max<uint32_t>(L.ntr, d.ntrie);
+        if (plans[i]->bags && plans[i]->bags->g != g)
+            return fail(SGE_BAD_INPUT, "plan %u uses bag relations built on another graph", i);
         if (d.k > SGE_MAX_K) return fail(SGE_UNSUPPORTED, "plan %u has k=%u", i, d.k);
     }
     // pinned-list tables: a bitmap over all vertices when it fits in 4 KB.
@@ -2133,7 +2253,7 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
         const uint32_t choices[2] = {COUNT_MAX_WARPS, 2};
         for (uint32_t wpb : choices) {
             if (o.warps_per_block && wpb != std::min<uint32_t>(o.warps_per_block, COUNT_MAX_WARPS)) continue;
-            const size_t smem = warp_smem_bytes(L.tw, L.ntd, L.cs, L.nvs) * wpb;
+            const size_t smem = warp_smem_bytes(L.tw, L.ntd, L.cs, L.nvs, L.ntr) * wpb;
             int b = 0;
             // static (plan copies) + dynamic shared memory exceed the 48 KB default: opt in
             CUDA_TRY(cudaFuncSetAttribute(count_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -2144,7 +2264,7 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
         }
         if (o.warps_per_block && best_warps < 0) {
             L.wpb = std::min<uint32_t>(std::max<uint32_t>(o.warps_per_block, 1), COUNT_MAX_WARPS);
-            L.smem = warp_smem_bytes(L.tw, L.ntd, L.cs, L.nvs) * L.wpb;
+            L.smem = warp_smem_bytes(L.tw, L.ntd, L.cs, L.nvs, L.ntr) * L.wpb;
         }
         L.threads = L.wpb * 32;
         CUDA_TRY(cudaFuncSetAttribute(count_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
@@ -2252,11 +2372,11 @@ sge_status enqueue_launch(sge_graph *g, const LaunchCfg &L, unsigned char *B, ui
         if (L.want_stats)
             count_kernel<true><<<(unsigned)L.blocks, L.threads, L.smem, s>>>(
                 dg, dplans, L.nplans, dqueue, dcounts, scratch, L.cap, L.nbufs, L.tw, L.tmode, L.deadline, dflags,
-                dstats, phase, H, L.ntd, L.cs, L.nvs);
+                dstats, phase, H, L.ntd, L.cs, L.nvs, L.ntr);
         else
             count_kernel<false><<<(unsigned)L.blocks, L.threads, L.smem, s>>>(
                 dg, dplans, L.nplans, dqueue, dcounts, scratch, L.cap, L.nbufs, L.tw, L.tmode, L.deadline, dflags,
-                dstats, phase, H, L.ntd, L.cs, L.nvs);
+                dstats, phase, H, L.ntd, L.cs, L.nvs, L.ntr);
         CUDA_TRY(cudaGetLastError());
         ++launches;
     }
@@ -2665,6 +2785,7 @@ sge_status sge_enumerate(sge_graph *g, const sge_plan *p, uint32_t *d_out, uint6
     CUDA_TRY(cudaSetDevice(g->device));
     DevPlan d = p->dp;
     d.ne = d.k;  // every level is enumerated
+    d.ntrie = 0;
     d.hoist_mask = 0;
     d.root_stride = 1;
     d.root_offset = 0;
@@ -2882,3 +3003,260 @@ extern "C" sge_status sge_count_noalloc(const uint32_t *d_offsets, const uint32_
         return fail(SGE_STACK_OVERFLOW, "a candidate list exceeded max_degree %u (pass a true upper bound)", max_degree);
     return SGE_OK;
 }
+
+// ---- bag relations ----
+namespace {
+
+// first[v] = first level-1 node under key v: the child offset of the first
+// level-0 node with value >= v (all level-1 nodes when there is none).
+__global__ void trie_first_kernel(const uint32_t *val0, const unsigned long long *child0, unsigned long long len0,
+                                  unsigned long long len1, uint32_t n, unsigned long long *first) {
+    const unsigned long long v = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (v > n) return;
+    unsigned long long lo = 0, w = len0;
+    while (w > 0) {
+        const unsigned long long half = w >> 1;
+        if (val0[lo + half] < v) { lo += half + 1; w -= half + 1; }
+        else w = half;
+    }
+    first[v] = lo < len0 ? child0[lo] : len1;
+}
+
+void free_rel(BagRel &r) {
+    sge_trie_free(&r.trie);
+    cudaFree(r.first);
+    r.first = nullptr;
+}
+
+// The bag's sub-pattern planned for all of its embeddings: no symmetry
+// restrictions, both orientations of every root edge, every earlier level
+// that is not a parent excluded (injectivity).
+void strip_restrictions(sge_plan_blob &b) {
+    for (uint32_t i = 0; i < SGE_MAX_K; ++i) b.lower[i] = b.upper[i] = 0;
+    b.root_kind = SGE_ROOT_ANY;
+    for (uint32_t i = 1; i < b.k; ++i) {
+        const uint32_t below = i < b.num_enum ? (1u << i) - 1u : (1u << b.num_enum) - 1u;
+        b.check[i] = below & ~b.parents[i];
+    }
+    b.num_restrictions = 0;
+    b.count_multiplier = 1;
+    b.single_bag = 0;
+}
+
+// One relation: count its tuples, enumerate them, sort, build the trie and
+// its dense first level.  *skipped is set (and nothing built) when the
+// relation holds more than max_rows tuples.
+sge_status build_rel(sge_graph *g, const sge_plan_blob &blob, uint32_t arity, uint64_t max_rows, size_t bag,
+                     BagRel &r, bool *skipped) {
+    *skipped = false;
+    sge_plan *sp = nullptr;
+    sge_status st = sge_plan_create(&blob, &sp);
+    if (st != SGE_OK) return st;
+    uint64_t cnt = 0, rows = 0;
+    const sge_plan *cp = sp;
+    st = sge_count(g, &cp, 1, nullptr, &cnt, &rows, nullptr);
+    if (st == SGE_OK && rows > max_rows) {
+        sge_plan_destroy(sp);
+        *skipped = true;
+        return SGE_OK;
+    }
+    uint32_t *d = nullptr;
+    if (st == SGE_OK && rows) {
+        cudaError_t e = cudaMalloc(&d, rows * arity * 4ull);
+        if (e != cudaSuccess) st = fail(SGE_OOM, "bag %zu: %llu tuples: %s", bag, (unsigned long long)rows, cudaGetErrorString(e));
+    }
+    uint64_t n2 = 0;
+    if (st == SGE_OK && rows) st = sge_enumerate(g, sp, d, rows, &n2);
+    if (st == SGE_OK && rows && n2 != rows)
+        st = fail(SGE_CUDA_ERROR, "bag %zu: enumerated %llu tuples, counted %llu", bag, (unsigned long long)n2,
+                  (unsigned long long)rows);
+    if (st == SGE_OK && rows) st = sge_sort_tuples(d, rows, arity);
+    if (st == SGE_OK) st = sge_trie_build(d, rows, arity, &r.trie);
+    cudaFree(d);
+    sge_plan_destroy(sp);
+    if (st != SGE_OK) return st;
+    r.rows = rows;
+    CUDA_TRY(cudaMalloc(&r.first, 8ull * (g->n + 1)));
+    if (rows == 0) {
+        CUDA_TRY(cudaMemset(r.first, 0, 8ull * (g->n + 1)));
+    } else {
+        trie_first_kernel<<<(unsigned)((g->n + 256) / 256), 256>>>(r.trie.values[0], r.trie.child[0],
+                                                                  r.trie.level_len[0], r.trie.level_len[1], g->n,
+                                                                  r.first);
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaDeviceSynchronize());
+    }
+    return SGE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+sge_status sge_bags_create(sge_graph *g, uint32_t k, uint32_t m, const uint32_t *edges, const char *plan_text,
+                           uint64_t max_rows, sge_bags **out) {
+    if (!g || !edges || !plan_text || !out) return fail(SGE_BAD_INPUT, "sge_bags_create: null argument");
+    *out = nullptr;
+    if (k < 3 || k > SGE_MAX_K) return fail(SGE_BAD_INPUT, "pattern k=%u outside 3..%u", k, SGE_MAX_K);
+    uint32_t adj[SGE_MAX_K] = {};
+    for (uint32_t e = 0; e < m; ++e) {
+        const uint32_t a = edges[2 * e], b = edges[2 * e + 1];
+        if (a >= k || b >= k || a == b) return fail(SGE_BAD_INPUT, "pattern edge %u (%u,%u) is invalid", e, a, b);
+        adj[a] |= 1u << b;
+        adj[b] |= 1u << a;
+    }
+    std::vector<std::vector<uint32_t>> bags;
+    sge_status st = parse_bag_text(k, plan_text, bags);
+    if (st != SGE_OK) return st;
+    std::vector<uint32_t> mask(bags.size(), 0);
+    for (size_t b = 0; b < bags.size(); ++b)
+        for (uint32_t u : bags[b]) mask[b] |= 1u << u;
+    DeviceGuard restore_device;
+    CUDA_TRY(cudaSetDevice(g->device));
+    sge_bags *B = new sge_bags();
+    B->g = g;
+    B->device = g->device;
+    B->k = k;
+    auto bail = [&](sge_status s) {
+        sge_bags_destroy(B);
+        return s;
+    };
+    // every bag but the global one (printed last)
+    for (size_t b = 0; b + 1 < bags.size(); ++b) {
+        uint32_t others = 0;
+        for (size_t c = 0; c < bags.size(); ++c)
+            if (c != b) others |= mask[c];
+        const uint32_t own = mask[b] & ~others;
+        const uint32_t size = (uint32_t)__builtin_popcount(mask[b]);
+        if (__builtin_popcount(own) != 1 || size < 3 || size > 4) continue;
+        BagRel r;
+        r.priv = (uint32_t)__builtin_ctz(own);
+        if (adj[r.priv] & ~mask[b]) continue;  // (a decomposition keeps a vertex's edges in its only bag)
+        uint32_t col[SGE_MAX_K];
+        for (uint32_t msk = mask[b] & ~own; msk; msk &= msk - 1) {
+            const uint32_t u = (uint32_t)__builtin_ctz(msk);
+            col[u] = r.nkeys;
+            r.keys[r.nkeys++] = u;
+        }
+        col[r.priv] = r.nkeys;
+        std::vector<uint32_t> sub;
+        for (uint32_t e = 0; e < m; ++e) {
+            const uint32_t a = edges[2 * e], c = edges[2 * e + 1];
+            if (((mask[b] >> a) & 1u) && ((mask[b] >> c) & 1u)) { sub.push_back(col[a]); sub.push_back(col[c]); }
+        }
+        sge_plan_opts o{};
+        o.join_style = SGE_JOIN_WCOJ;
+        o.use_iep = 0;
+        o.max_tail = 1;
+        sge_plan_blob blob;
+        // a bag whose sub-pattern is not connected is not planned (its tail
+        // level keeps intersecting adjacency lists)
+        if (sge_plan_pattern_stats(size, (uint32_t)sub.size() / 2, sub.data(), &g->stats, &o, &blob) != SGE_OK) continue;
+        strip_restrictions(blob);
+        // (the sort and the trie index rows with 32 bits)
+        const uint64_t cap = std::min<uint64_t>(max_rows ? max_rows : ~0ull, 0xFFFFFFFFull);
+        bool skipped = false;
+        st = build_rel(g, blob, size, cap, b, r, &skipped);
+        if (st != SGE_OK) {
+            free_rel(r);
+            return bail(st);
+        }
+        if (skipped) {
+            ++B->skipped;
+            continue;
+        }
+        B->bytes += 8ull * (g->n + 1);
+        for (uint32_t l = 0; l < size; ++l)
+            B->bytes += 4ull * r.trie.level_len[l] + (l + 1 < size ? 8ull * (r.trie.level_len[l] + 1) : 0ull);
+        B->rels.push_back(r);
+    }
+    if (!B->rels.empty()) {
+        std::vector<DevTrie> dt(B->rels.size());
+        for (size_t i = 0; i < B->rels.size(); ++i) {
+            const BagRel &r = B->rels[i];
+            DevTrie &t = dt[i];
+            memset(&t, 0, sizeof t);
+            t.first = r.first;
+            t.nkeys = r.nkeys;
+            for (uint32_t l = 1; l <= r.nkeys; ++l) t.val[l] = r.trie.values[l];
+            for (uint32_t l = 1; l < r.nkeys; ++l) t.child[l] = r.trie.child[l];
+        }
+        cudaError_t e = cudaMalloc(&B->d_tries, sizeof(DevTrie) * dt.size());
+        if (e == cudaSuccess) e = cudaMemcpy(B->d_tries, dt.data(), sizeof(DevTrie) * dt.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return bail(fail(SGE_CUDA_ERROR, "sge_bags_create: %s", cudaGetErrorString(e)));
+    }
+    *out = B;
+    return SGE_OK;
+}
+
+sge_status sge_bags_info(const sge_bags *b, uint32_t *num_relations, uint64_t *rows, uint64_t *device_bytes,
+                         uint32_t *own_vertices, uint32_t *num_skipped) {
+    if (!b) return fail(SGE_BAD_INPUT, "sge_bags_info: null bags");
+    uint64_t total = 0;
+    for (size_t i = 0; i < b->rels.size(); ++i) {
+        total += b->rels[i].rows;
+        if (own_vertices) own_vertices[i] = b->rels[i].priv;
+    }
+    if (num_relations) *num_relations = (uint32_t)b->rels.size();
+    if (rows) *rows = total;
+    if (device_bytes) *device_bytes = b->bytes;
+    if (num_skipped) *num_skipped = b->skipped;
+    return SGE_OK;
+}
+
+sge_status sge_bags_destroy(sge_bags *b) {
+    if (!b) return SGE_OK;
+    DeviceGuard restore_device;
+    cudaSetDevice(b->device);
+    for (auto &r : b->rels) free_rel(r);
+    cudaFree(b->d_tries);
+    delete b;
+    return SGE_OK;
+}
+
+sge_status sge_plan_use_bags(sge_plan *p, const sge_bags *b, uint32_t *levels) {
+    if (!p) return fail(SGE_BAD_INPUT, "sge_plan_use_bags: null plan");
+    if (levels) *levels = 0;
+    // back to the plan's own device form (its tuning is kept)
+    to_devplan(p->blob, p->dp);
+    p->bags = nullptr;
+    if (!b) return SGE_OK;
+    const sge_plan_blob &bl = p->blob;
+    if (b->k != bl.k) return fail(SGE_BAD_INPUT, "bags of a %u-vertex pattern, plan of %u vertices", b->k, bl.k);
+    if (bl.join_style != SGE_JOIN_WCOJ) return fail(SGE_UNSUPPORTED, "bag relations need a WCOJ plan");
+    uint32_t level_of[SGE_MAX_K];
+    for (uint32_t i = 0; i < bl.k; ++i) level_of[bl.order[i]] = i;
+    DevPlan &d = p->dp;
+    for (uint32_t i = 0; i < SGE_MAX_K; ++i) d.tri[i] = -1;
+    uint32_t j = 0;
+    for (size_t ri = 0; ri < b->rels.size() && j < 2; ++ri) {
+        const BagRel &r = b->rels[ri];
+        const uint32_t li = level_of[r.priv];
+        if (li < bl.num_enum) continue;  // its own vertex is enumerated, not a tail level
+        bool keyed = true;
+        for (uint32_t c = 0; c < r.nkeys; ++c) keyed &= level_of[r.keys[c]] < bl.num_enum;
+        if (!keyed) continue;
+        d.tri[li] = (int8_t)j;
+        d.trel[j] = (uint8_t)ri;
+        for (uint32_t c = 0; c < r.nkeys; ++c) d.tkey[j][c] = (uint8_t)level_of[r.keys[c]];
+        d.hoist_mask &= ~(1u << li);  // the trie replaces the hoisted intersection
+        ++j;
+    }
+    if (j == 0) return SGE_OK;
+    d.ntrie = j;
+    d.tries = b->d_tries;
+    d.pair_direct = 0;
+    // N(m[0]) / N(m[1]) / level 2's list stay pinned only for levels that still probe them
+    d.pin_mask = 0;
+    if (bl.num_enum >= 3)
+        for (uint32_t i = 3; i < bl.k; ++i) {
+            if (i >= bl.num_enum && d.tri[i] >= 0) continue;
+            d.pin_mask |= bl.parents[i] & 3u;
+            if (bl.base[i] == 2) d.pin_mask |= 4u;
+        }
+    p->bags = b;
+    if (levels) *levels = j;
+    return SGE_OK;
+}
+
+}  // extern "C"

@@ -757,14 +757,8 @@ static bool parse_order_line(const char *s, const char *e, std::vector<uint32_t>
     return any && !out.empty();
 }
 
-extern "C" sge_status sge_plan_from_order_text(uint32_t k, uint32_t m, const uint32_t *edges, const char *text,
-                                               const sge_graph_stats *stats, const sge_plan_opts *opts,
-                                               sge_plan_blob *out, uint32_t *num_bags) {
-    if (!text || !out || !edges) return fail(SGE_BAD_INPUT, "sge_plan_from_order_text: null argument");
-    Pattern p;
-    sge_status st = make_pattern(k, m, edges, p);
-    if (st != SGE_OK) return st;
-    std::vector<std::vector<uint32_t>> bags;
+sge_status sge::parse_bag_text(uint32_t k, const char *text, std::vector<std::vector<uint32_t>> &bags) {
+    bags.clear();
     long want = -1;  // from "num bags: N"
     std::vector<uint32_t> row;
     for (const char *s = text; *s;) {
@@ -782,18 +776,36 @@ extern "C" sge_status sge_plan_from_order_text(uint32_t k, uint32_t m, const uin
     if (bags.empty()) return fail(SGE_BAD_INPUT, "plan text holds no bag order");
     if (want >= 0 && (long)bags.size() != want)
         return fail(SGE_BAD_INPUT, "plan text announces %ld bags but holds %zu orders", want, bags.size());
-    // every attribute is a pattern vertex, once per bag; the bags cover the
-    // vertices and every pattern edge lies inside some bag (a decomposition)
+    // every attribute is a pattern vertex, once per bag; the bags cover the vertices
     uint32_t covered = 0;
-    std::vector<uint32_t> bag_mask(bags.size(), 0);
-    for (size_t b = 0; b < bags.size(); ++b)
+    for (size_t b = 0; b < bags.size(); ++b) {
+        uint32_t mask = 0;
         for (uint32_t u : bags[b]) {
             if (u >= k) return fail(SGE_BAD_INPUT, "bag %zu names vertex %u of a %u-vertex pattern", b, u, k);
-            if ((bag_mask[b] >> u) & 1u) return fail(SGE_BAD_INPUT, "bag %zu names vertex %u twice", b, u);
-            bag_mask[b] |= 1u << u;
-            covered |= 1u << u;
+            if ((mask >> u) & 1u) return fail(SGE_BAD_INPUT, "bag %zu names vertex %u twice", b, u);
+            mask |= 1u << u;
         }
+        covered |= mask;
+    }
     if (covered != ((1u << k) - 1u)) return fail(SGE_BAD_INPUT, "the bags do not cover every pattern vertex");
+    return SGE_OK;
+}
+
+extern "C" sge_status sge_plan_from_order_text(uint32_t k, uint32_t m, const uint32_t *edges, const char *text,
+                                               const sge_graph_stats *stats, const sge_plan_opts *opts,
+                                               sge_plan_blob *out, uint32_t *num_bags) {
+    if (!text || !out || !edges) return fail(SGE_BAD_INPUT, "sge_plan_from_order_text: null argument");
+    if (k < 3 || k > SGE_MAX_K) return fail(SGE_BAD_INPUT, "pattern k=%u outside 3..%u", k, SGE_MAX_K);
+    Pattern p;
+    sge_status st = make_pattern(k, m, edges, p);
+    if (st != SGE_OK) return st;
+    std::vector<std::vector<uint32_t>> bags;
+    st = parse_bag_text(k, text, bags);
+    if (st != SGE_OK) return st;
+    // every pattern edge lies inside some bag (a decomposition)
+    std::vector<uint32_t> bag_mask(bags.size(), 0);
+    for (size_t b = 0; b < bags.size(); ++b)
+        for (uint32_t u : bags[b]) bag_mask[b] |= 1u << u;
     for (uint32_t a = 0; a < k; ++a)
         for (uint32_t c = a + 1; c < k; ++c) {
             if (!p.edge(a, c)) continue;

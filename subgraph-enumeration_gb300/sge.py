@@ -176,6 +176,10 @@ SIGNATURES = {
     "sge_match_set": (C.c_int, [C.c_void_p, C.c_void_p, u32, u32, _P(u32), _P(u32), u64, _P(u64)]),
     "sge_count_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, u32, u64, u32, _P(PlanBlob), u32, C.c_void_p,
                                     C.c_void_p]),
+    "sge_bags_create": (C.c_int, [C.c_void_p, u32, u32, _P(u32), C.c_char_p, u64, _P(C.c_void_p)]),
+    "sge_bags_info": (C.c_int, [C.c_void_p, _P(u32), _P(u64), _P(u64), _P(u32), _P(u32)]),
+    "sge_bags_destroy": (C.c_int, [C.c_void_p]),
+    "sge_plan_use_bags": (C.c_int, [C.c_void_p, C.c_void_p, _P(u32)]),
 }
 
 
@@ -570,7 +574,7 @@ class Engine:
               max_level_capacity: int = 0, blocks_per_sm: int = 0, warps_per_block: int = 0, chunk: int = 0,
               root_stride: int = 1, root_offset: int = 0, heavy_threshold: int = 0, hub_bitmaps: bool = True,
               root_max_degree: int = 0, pin_tables: int = 0, tuning: "list[PlanTuning | None] | None" = None,
-              plan_times: bool = False):
+              plan_times: bool = False, bags: "list[Bags | None] | None" = None):
         """Counts every plan over the graph in one launch.  Returns (counts,
         instances, stats-dict); counts are the reference's "Number of matches"
         (uint64).  stats=True runs the instrumented kernel (set operations,
@@ -585,8 +589,12 @@ class Engine:
         tables on large graphs (sge_count_opts.pin_tables); tuning
         gives each plan its PlanTuning (None = automatic).  plan_times=True
         also returns stats["plan_busy_ms"]: per plan, the warp-milliseconds
-        its roots took (sge_count_plan_times; instances are then not read)."""
+        its roots took (sge_count_plan_times; instances are then not read).
+        bags gives each plan the bag relations its tail levels read
+        (sge_plan_use_bags; None = intersect adjacency lists);
+        stats["bag_levels"] then lists, per plan, the tail levels that did."""
         handles = []
+        bag_levels = []
         try:
             for i, b in enumerate(plans):
                 ph = C.c_void_p()
@@ -594,6 +602,12 @@ class Engine:
                 handles.append(ph)
                 if tuning is not None and tuning[i] is not None:
                     _check(lib().sge_plan_set_tuning(ph, C.byref(tuning[i])))
+                if bags is not None and bags[i] is not None:
+                    lv = u32()
+                    _check(lib().sge_plan_use_bags(ph, bags[i]._h, C.byref(lv)))
+                    bag_levels.append(lv.value)
+                else:
+                    bag_levels.append(0)
             arr = (C.c_void_p * len(handles))(*[h.value for h in handles])
             counts = (u64 * len(plans))()
             inst = (u64 * len(plans))()
@@ -608,10 +622,20 @@ class Engine:
                 d["plan_busy_ms"] = list(busy)
                 return list(counts), [], d
             _check(lib().sge_count(self._h, arr, len(plans), C.byref(o), counts, inst, C.byref(st)))
-            return list(counts), list(inst), st.as_dict()
+            d = st.as_dict()
+            if bags is not None:
+                d["bag_levels"] = bag_levels
+            return list(counts), list(inst), d
         finally:
             for h in handles:
                 lib().sge_plan_destroy(h)
+
+    def bags(self, pattern: PatternGraph, text: str, max_rows: int = 0) -> "Bags":
+        """Bag relations of the decomposition in `text` on this graph
+        (sge_bags_create): each bag with one attribute of its own and 3 or 4
+        attributes, as a trie.  A bag with more than max_rows tuples (0 = no
+        limit) is skipped."""
+        return Bags(self, pattern, text, max_rows)
 
     def match_set(self, pattern: PatternGraph, exploration: bool = False, max_rows: int = 1 << 26) -> np.ndarray:
         """Sorted instance set: one row per instance (canonical image under the
@@ -640,6 +664,42 @@ class Engine:
     def close(self) -> None:
         if getattr(self, "_h", None):
             lib().sge_graph_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Bags:
+    """sge_bags: bag relations (tries) of a decomposition on one graph."""
+
+    def __init__(self, engine: Engine, pattern: PatternGraph, text: str, max_rows: int = 0):
+        self.engine = engine  # the relations belong to this graph: keep it alive
+        h = C.c_void_p()
+        e = pattern.flat()
+        _check(lib().sge_bags_create(engine._h, pattern.k, pattern.m, _u32p(e), text.encode(), max_rows,
+                                     C.byref(h)))
+        self._h = h
+
+    def info(self) -> dict:
+        n, rows, nbytes, skipped = u32(), u64(), u64(), u32()
+        own = (u32 * 16)()
+        _check(lib().sge_bags_info(self._h, C.byref(n), C.byref(rows), C.byref(nbytes), own, C.byref(skipped)))
+        return {"relations": n.value, "rows": rows.value, "device_bytes": nbytes.value,
+                "own_vertices": list(own)[: n.value], "skipped": skipped.value}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().sge_bags_destroy(self._h)
             self._h = None
 
     def __enter__(self):

@@ -6,7 +6,8 @@ Run with SGE_REFERENCE naming a reference checkout, after
 ``__graft_entry__.build()`` (same variable) has compiled
 oracle/_ref/graph_mining_system from its sources.  Writes
 tests/golden/golden_rmat.json: per (graph, pattern) the reference's
-"Number of matches", its "num bags" and run time.
+"Number of matches", its "num bags", the decomposition it printed
+(the text sge_plan_from_order_text and sge_bags_create read) and run time.
 """
 from __future__ import annotations
 
@@ -57,8 +58,13 @@ def main() -> None:
                                capture_output=True, text=True, timeout=600)
             m = re.search(r"Number of matches: (\d+)", r.stdout)
             b = re.search(r"num bags: (\d+)", r.stdout)
+            plan = None
+            if b:  # the printed decomposition: "num bags: N" and one order per bag
+                lines = r.stdout[b.start():].splitlines()
+                plan = "\n".join(lines[: 1 + int(b.group(1))]) + "\n"
             row = {"graph": gname, "pattern": pn, "count": int(m.group(1)) if m else None,
-                   "num_bags": int(b.group(1)) if b else None, "rc": r.returncode, "seconds": round(time.time() - t, 1)}
+                   "num_bags": int(b.group(1)) if b else None, "plan": plan, "rc": r.returncode,
+                   "seconds": round(time.time() - t, 1)}
             out["results"].append(row)
             print(row, flush=True)
     (HERE / "golden_rmat.json").write_text(json.dumps(out, indent=0))

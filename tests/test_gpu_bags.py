@@ -1,0 +1,151 @@
+"""The bag-relation join: tail levels that read their candidates from a bag's
+trie (sge_bags_create + sge_plan_use_bags) instead of intersecting adjacency
+lists.  The relation of a bag is all embeddings of its sub-pattern (the
+reference's nodeJoin tuples, matching/join.cpp:309-421) in a trie keyed by
+the bag's other attributes (buildTrie, join.cpp:1713-1717); the counts must
+not change.  Checked against the reference's own decompositions and counts
+(ca-netscience: the 214 recorded plans; down-scaled R-MAT: the plans it
+printed there), against the CPU oracle, and against a brute-force relation."""
+import json
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, pattern_of
+
+pytestmark = pytest.mark.gpu
+
+TWO_TRIANGLES_4CYCLE = (6, [(0, 1), (0, 2), (1, 2), (3, 4), (3, 5), (4, 5), (1, 3), (2, 4)])
+# a decomposition of it in the reference's printed form: vertices 0 and 5 are
+# the own attributes of the triangle bags (1,0,2) and (3,4,5); global bag last
+TWO_TRIANGLES_4CYCLE_BAGS = "num bags: 5\n1,0,2\n3,1,2\n3,4,2\n3,4,5\n3,4,1,2\n"
+
+
+@pytest.fixture(scope="module")
+def ca(sge):
+    return sge.DataGraph.load(GOLDEN / "ca_netscience.el")
+
+
+@pytest.fixture(scope="module")
+def gold_rmat():
+    return json.loads((GOLDEN / "golden_rmat.json").read_text())
+
+
+def rmat(sge, gold, name):
+    spec = gold["graphs"][name]
+    g = sge.gen_rmat(spec["scale"], spec["m"], spec["a"], spec["b"], spec["c"], spec["seed"])
+    assert g.fingerprint() == spec["fingerprint"]
+    return g
+
+
+def test_reference_plans_through_bag_relations(sge, patterns, ca, golden):
+    from test_plan_import import expected
+    rows = [r for r in json.loads((GOLDEN / "reference_plans.json").read_text())["rows"]
+            if r["rc"] == 0 and r["count"] is not None]
+    golden_default = {r["pattern"]: r["count"] for r in golden["results"]
+                      if r["graph"] == "ca_netscience" and r["mode"] == "default" and r["rc"] == 0}
+    plans, bags = [], []
+    with sge.Engine(ca) as eng:
+        for r in rows:
+            p = pattern_of(sge, patterns, r["pattern"])
+            b, _ = sge.plan_from_reference(p, r["plan"], ca, iep=r["mode"] == "u")
+            plans.append(b)
+            bags.append(eng.bags(p, r["plan"]))
+        counts, _, st = eng.count(plans, bags=bags)
+        plain, _, _ = eng.count(plans)
+        used = st["bag_levels"]
+        for bg in bags:
+            bg.close()
+    bad = [(r["pattern"], r["mode"], c) for r, c in zip(rows, counts) if c != expected(r, golden_default)]
+    assert not bad, bad[:5]
+    assert counts == plain
+    # half of the decompositions have a bag whose one own vertex is a tail level
+    assert sum(1 for u in used if u) >= 100, sum(1 for u in used if u)
+
+
+@pytest.mark.parametrize("graph", ["rmat_s14", "rmat_s16"])
+def test_reference_decompositions_on_downscaled_rmat(sge, patterns, gold_rmat, graph):
+    rows = [r for r in gold_rmat["results"] if r["graph"] == graph and r["rc"] == 0 and r.get("plan")
+            and r["num_bags"] > 1]
+    assert len(rows) >= 3
+    g = rmat(sge, gold_rmat, graph)
+    with sge.Engine(g) as eng:
+        any_used = skipped = 0
+        for r in rows:
+            p = pattern_of(sge, patterns, r["pattern"])
+            # relations of up to 3e8 tuples (wedges and K4s of these graphs hold
+            # 1.6e9-1.1e10 and are skipped: their levels keep intersecting)
+            with eng.bags(p, r["plan"], max_rows=300_000_000) as bg:
+                skipped += bg.info()["skipped"]
+                for iep in (False, True):
+                    b, _ = sge.plan_from_reference(p, r["plan"], eng, iep=iep)
+                    counts, _, st = eng.count([b], bags=[bg])
+                    assert counts[0] == r["count"], (r["pattern"], iep, counts[0], r["count"])
+                    any_used += st["bag_levels"][0]
+        assert any_used > 0 and skipped > 0
+
+
+def test_two_triangles_4cycle_against_the_oracle(sge, oracle, gold_rmat):
+    g = rmat(sge, gold_rmat, "rmat_s14")
+    p = sge.PatternGraph.from_edges(*TWO_TRIANGLES_4CYCLE)
+    with sge.Engine(g) as eng:
+        with eng.bags(p, TWO_TRIANGLES_4CYCLE_BAGS) as bg:
+            info = bg.info()
+            assert info["relations"] == 2 and sorted(info["own_vertices"]) == [0, 5]
+            for iep in (False, True):
+                b, nb = sge.plan_from_reference(p, TWO_TRIANGLES_4CYCLE_BAGS, eng, iep=iep)
+                assert nb == 5
+                full, _, st = eng.count([b], bags=[bg])
+                assert st["bag_levels"] == [2 if iep else 1]
+                assert full == eng.count([b])[0]
+                # a root sample, on the oracle too
+                stride = 64
+                s, _, _ = eng.count([b], bags=[bg], root_stride=stride, root_offset=3)
+                inst, _ = oracle.count_plan(g.offsets, g.nbrs, b, threads=0, stride=stride, offset=3)
+                assert s[0] == inst * b.count_multiplier and s[0] > 0
+
+
+def test_relation_is_every_embedding_of_the_bag(sge, graphs):
+    g = graphs("ca_netscience")
+    tri = sge.PatternGraph.from_edges(3, [(0, 1), (0, 2), (1, 2)])
+    # pattern: a triangle (1,0,2) with a pendant path: bag (1,0,2) owns 0
+    p = sge.PatternGraph.from_edges(4, [(0, 1), (0, 2), (1, 2), (2, 3)])
+    with sge.Engine(g) as eng:
+        with eng.bags(p, "num bags: 2\n1,0,2\n2,3,1\n") as bg:
+            info = bg.info()
+        tri_emb = eng.count([sge.plan(tri, eng)])[0][0]  # embeddings (one bag)
+    assert info["relations"] == 1 and info["own_vertices"] == [0]
+    assert info["rows"] == tri_emb and tri_emb > 0
+    # brute force: ordered triangles of the CSR
+    off, nb = g.offsets, g.nbrs
+    adj = [set(nb[off[v]:off[v + 1]].tolist()) for v in range(g.num_vertices)]
+    n = sum(len(adj[a] & adj[b]) for a in range(g.num_vertices) for b in adj[a])
+    assert n == tri_emb
+
+
+def test_bag_errors(sge, graphs):
+    g = graphs("ca_netscience")
+    p = sge.PatternGraph.from_edges(*TWO_TRIANGLES_4CYCLE)
+    q = sge.PatternGraph.from_edges(4, [(0, 1), (0, 2), (1, 2), (2, 3)])
+    with sge.Engine(g) as eng, sge.Engine(g) as other:
+        with pytest.raises(sge.SgeError) as e:
+            eng.bags(p, "num bags: 2\n0,1,2\n")
+        assert e.value.status_name == "BAD_INPUT"
+        with eng.bags(p, TWO_TRIANGLES_4CYCLE_BAGS, max_rows=10) as small:  # both relations too large
+            assert small.info()["relations"] == 0 and small.info()["skipped"] == 2
+            b, _ = sge.plan_from_reference(p, TWO_TRIANGLES_4CYCLE_BAGS, eng)
+            c, _, st = eng.count([b], bags=[small])
+            assert st["bag_levels"] == [0] and c == eng.count([b])[0]
+        with eng.bags(p, TWO_TRIANGLES_4CYCLE_BAGS) as bg:
+            b, _ = sge.plan_from_reference(p, TWO_TRIANGLES_4CYCLE_BAGS, eng)
+            with pytest.raises(sge.SgeError) as e:  # relations of another graph
+                other.count([b], bags=[bg])
+            assert e.value.status_name == "BAD_INPUT"
+            bq = sge.plan(q, eng)
+            with pytest.raises(sge.SgeError) as e:  # another pattern
+                eng.count([bq], bags=[bg])
+            assert e.value.status_name == "BAD_INPUT"
+            be, _ = sge.plan_from_reference(p, TWO_TRIANGLES_4CYCLE_BAGS, eng, exploration=True)
+            with pytest.raises(sge.SgeError) as e:
+                eng.count([be], bags=[bg])
+            assert e.value.status_name == "UNSUPPORTED"

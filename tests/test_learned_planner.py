@@ -94,3 +94,25 @@ def test_learned_scorer_beats_cost_model_on_held_out_patterns(sge):
     shipped = sge_learn.load_mlp(PKG / "scorer" / "mlp_weights.npz")
     rs = sge_learn.regret(te, shipped)
     assert rs["learned"] <= rs["cost_model"], rs
+
+
+@pytest.mark.gpu
+def test_shipped_scorer_on_the_benchmark_setting(sge):
+    """The shipped weights were trained on both recordings; on the held-out
+    patterns of the R-MAT 2^22 recording (the benchmark's graph and root
+    sample, tests/golden/make_plan_runtimes.py --rmat22) they pick plans no
+    slower than the cost model's choice."""
+    import sge_learn
+    fx = GOLDEN / "plan_runtimes_rmat22.npz"
+    meta = json.loads(fx.with_suffix(".json").read_text())
+    rec = sge_learn.Records.load(fx)
+    held = {m["id"] for m in meta["patterns"] if not m["train"]}
+    te = sge_learn.Records()
+    for i in range(len(rec.pattern)):
+        if rec.pattern[i] in held:
+            te.pattern.append(rec.pattern[i]); te.cand.append(rec.cand[i]); te.x.append(rec.x[i])
+            te.ms.append(rec.ms[i]); te.count.append(rec.count[i])
+    shipped = sge_learn.load_mlp(PKG / "scorer" / "mlp_weights.npz")
+    rs = sge_learn.regret(te, shipped)
+    assert rs["patterns"] >= 10
+    assert rs["learned"] <= rs["cost_model"], rs
