@@ -223,14 +223,16 @@ def sample_opts(world: int = 1, rank: int = 0, sub: int = 1) -> dict:
                 root_max_degree=ROOT_MAX_DEGREE)
 
 
-def rmat22_config(extra: dict | None = None) -> dict:
-    c = {"workload": f"rmat_s22_m64M x 78 random 7-vertex patterns (16-19 edges), root sample: undirected edges "
-                     f"e = {SAMPLE_OFFSET} mod {SAMPLE_STRIDE} (CSR order, both orientations) with both endpoint "
-                     f"degrees <= {ROOT_MAX_DEGREE}",
+def rmat22_config(extra: dict | None = None, scale: int = RMAT22["scale"], npat: int = N_PATTERNS) -> dict:
+    size = "m64M" if scale == RMAT22["scale"] else f"m{(16 << scale) // 1_000_000}M"
+    c = {"workload": f"rmat_s{scale}_{size} x {npat} random 7-vertex patterns (16-19 edges), root sample: undirected "
+                     f"edges e = {SAMPLE_OFFSET} mod {SAMPLE_STRIDE} (CSR order, both orientations) with both "
+                     f"endpoint degrees <= {ROOT_MAX_DEGREE}",
          "graph": dict(RMAT22, generator="rmat", ids="unpermuted", built="on the GPU (sge_graph_create_rmat)"),
          "patterns": "PatternGraph.random(7, 16 + i % 4, 2000 + i), i < 78",
          "root_sample": {"stride": SAMPLE_STRIDE, "offset": SAMPLE_OFFSET, "max_endpoint_degree": ROOT_MAX_DEGREE,
-                         "edges_before_degree_cap": RMAT22["m"] // SAMPLE_STRIDE},
+                         "edges_before_degree_cap": (RMAT22["m"] if scale == RMAT22["scale"] else 16 << scale)
+                         // SAMPLE_STRIDE},
          "symmetry": "per pattern one restriction sequence and root edge for every plan (canonical_symmetry)",
          "l2": "inputs larger than L2 (512 MB CSR + 4 GB hub bitmaps); 512 MiB L2 flush before each timed step",
          "parallelism": "root-edge sharding across ranks"}
@@ -510,7 +512,7 @@ def run_rmat22(args):
                                  "patterns_used": len(pats),
                                  "ingest_s": ingest_s, "hub_index": {"hubs": info["hub_count"],
                                                                       "min_degree": info["hub_min_degree"]},
-                                 "max_degree": info["max_degree"]}),
+                                 "max_degree": info["max_degree"]}, g["scale"], len(pats)),
         "learned_batched": {"wall_s": lw, "planning_s": lp, "kernel_ms": lk, "value_wall": total / lw,
                             "note": "planning + one launch with the automatic settings"},
         "autotuner": {"tuning_s": tune_s, "tuning_kernel_ms": tuned.tuning_ms, "runs": tuned.runs,
@@ -737,7 +739,12 @@ def run_bags(args):
     opts = dict(root_stride=args.bag_stride, root_offset=0)
     for name, ((k, edges), text) in BAG_PATTERNS.items():
         p = sge.PatternGraph.from_edges(k, edges)
-        b, nb = sge.plan_from_reference(p, text, eng, iep=True)
+        imp, nb = sge.plan_from_reference(p, text, eng, iep=True)
+        # the imported order with its longest tail, so every bag's own vertex is
+        # a tail level (the cost model may enumerate one instead)
+        cands = sge.candidates(p, eng.graph.stats(), cap=64, force_order=list(imp.order[:k]))
+        b = max(cands, key=lambda x: x.tail_len)
+        b.count_multiplier, b.single_bag, b.choose_wrap = imp.count_multiplier, imp.single_bag, 1
         t0 = time.perf_counter()
         try:
             bags = eng.bags(p, text, max_rows=args.bag_max_rows)
@@ -748,15 +755,24 @@ def run_bags(args):
         info = bags.info()
         res = {}
         for arm, bg in (("dfs", None), ("trie", bags)):
-            for _ in range(args.warmup):
-                c, _, st = eng.count([b], bags=[bg], **opts)
             ms = []
-            for _ in range(args.steps):
-                c, _, st = eng.count([b], bags=[bg], **opts)
-                ms.append(st["kernel_ms"])
+            try:
+                for i in range(args.warmup + args.steps):
+                    c, _, st = eng.count([b], bags=[bg], time_budget_s=args.bag_budget_s, **opts)
+                    if i >= args.warmup:
+                        ms.append(st["kernel_ms"])
+            except sge.SgeError as e:
+                res[arm] = (None, None, str(e))
+                continue
             res[arm] = (c[0], statistics.median(ms), st.get("bag_levels", [0])[0])
+        if res["dfs"][0] is None or res["trie"][0] is None:
+            rows.append({"pattern": name, "bags": nb, "dfs": res["dfs"], "trie": res["trie"],
+                         "relation_build_s": round(build_s, 3)})
+            bags.close()
+            continue
         assert res["dfs"][0] == res["trie"][0], (name, res)
-        rows.append({"pattern": name, "bags": nb, "count": res["dfs"][0], "trie_levels": res["trie"][2],
+        rows.append({"pattern": name, "bags": nb, "order": list(b.order[:k]), "tail_len": b.tail_len,
+                     "count": res["dfs"][0], "trie_levels": res["trie"][2],
                      "relations": info["relations"], "relation_rows": info["rows"],
                      "relation_bytes": info["device_bytes"], "relation_build_s": round(build_s, 3),
                      "dfs_kernel_ms": res["dfs"][1], "trie_kernel_ms": res["trie"][1],
@@ -768,7 +784,8 @@ def run_bags(args):
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "data": "synthetic", "dtype": "u32 ids",
             "config": {"workload": f"rmat_s{scale} bags", "graph": dict(scale=scale, m=16 << scale, a=0.57, b=0.19,
                                                                        c=0.19, seed=4, generator="rmat"),
-                       "root_stride": args.bag_stride, "leaf": "inclusion-exclusion (-u)"},
+                       "root_sample": f"undirected root edges e = 0 mod {args.bag_stride}",
+                       "plan": "the imported decomposition's order with its longest tail"},
             "rows": rows}
     print(json.dumps(line), flush=True)
 
@@ -790,7 +807,8 @@ def main():
                     help="rmat22: per-level list capacity (0 = max degree; smaller values bound device memory "
                          "for profiling captures; a list past it fails loudly)")
     ap.add_argument("--bag-scale", type=int, default=16, help="bags: R-MAT scale (16·2^scale edges)")
-    ap.add_argument("--bag-stride", type=int, default=1, help="bags: root sample stride (1 = every root)")
+    ap.add_argument("--bag-stride", type=int, default=64, help="bags: root sample stride (1 = every root)")
+    ap.add_argument("--bag-budget-s", type=float, default=60.0, help="bags: time budget of one count")
     ap.add_argument("--bag-max-rows", type=int, default=4_000_000_000, help="bags: tuples per relation at most")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -64,6 +64,8 @@ def lib() -> C.CDLL:
         L.oracle_csr_from_sorted_edges.argtypes = [_P(u32), u64, u32, _P(u32), _P(u32)]
         L.oracle_free.restype = None
         L.oracle_free.argtypes = [C.c_void_p]
+        L.oracle_alg_bytes_root_leaf.restype = u64
+        L.oracle_alg_bytes_root_leaf.argtypes = [_P(u32), _P(u32), u32, C.c_void_p, u64, u64, u32, u32]
         _lib = L
     return _lib
 
@@ -243,3 +245,16 @@ def gen_chung_lu(n: int, m: int, gamma: float, max_deg: int = 0, seed: int = 0) 
     if not lib().oracle_gen_chung_lu(n, m, round(gamma * 1000), max_deg, seed, C.byref(ep), C.byref(mo)):
         raise ValueError("oracle_gen_chung_lu: bad arguments")
     return csr_from_sorted_edges(_take_edges(ep, mo.value), n)
+
+
+def alg_bytes_root_leaf(offsets, nbrs, blob, stride: int = 1, offset: int = 0, root_max_degree: int = 0,
+                        hub_min: int = 0xFFFFFFFF) -> int:
+    """The instrumented kernel's algorithmic bytes for a WCOJ plan with two
+    enumerated levels, from the counter's definition (sge_oracle.c, part 5);
+    hub_min is the graph's hub threshold (0xFFFFFFFF: no hub bitmaps)."""
+    off, nb = _arr(offsets), _arr(nbrs)
+    r = lib().oracle_alg_bytes_root_leaf(_p(off), _p(nb), off.size - 1, C.addressof(blob), stride, offset,
+                                         root_max_degree, hub_min)
+    if r == (1 << 64) - 1:
+        raise ValueError("alg_bytes_root_leaf needs a WCOJ plan with two enumerated levels")
+    return int(r)

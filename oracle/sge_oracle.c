@@ -15,7 +15,10 @@
  *     following the reference's join structure (generateCandidates →
  *     MultiIntersection → DFS; traverse → numResults / choosec /
  *     numUniqueCombine at the leaf), parallel over root edges with OpenMP like
- *     parSharedJoin (matching/parallel.cpp:1154-1486).
+ *     parSharedJoin (matching/parallel.cpp:1154-1486);
+ *  4. copies of the library's seeded generators and CSR build;
+ *  5. the definition of the instrumented kernel's algorithmic-byte counter
+ *     for plans whose leaf runs on the root edge, evaluated on the CPU.
  */
 #include <math.h>
 #include <stdint.h>
@@ -932,3 +935,126 @@ void oracle_csr_from_sorted_edges(const uint32_t *edges, uint64_t m, uint32_t n,
 }
 
 void oracle_free(void *p) { free(p); }
+
+/* ---------------------------------------------------------------- 5 ---- */
+/* Algorithmic bytes (the instrumented device kernel's alg_bytes counter) of a
+ * WCOJ plan with two enumerated levels, the root edge and its leaf, computed
+ * on the CPU from the counter's definition so the device figure can be
+ * checked.  The definition:
+ *  - root tasks t = 0.. (undirected edge offset + (t/2)·stride, t odd the
+ *    reversed orientation, for an unordered root; edge offset + t·stride
+ *    otherwise) are taken in groups of 32 in task order, roots the degree cap
+ *    drops removed from their group;
+ *  - a tail level counted with a scan scans, for every root of the group, the
+ *    same one of its lists: the one with the least Σ_roots len × (Σ of the
+ *    other lists' probe costs + 1), the first on ties, where a list's probe
+ *    cost is 1 for a list of at least hub_min entries (a hub bitmap) and
+ *    2 + ⌊log2(len+1)⌋ otherwise.  A root then costs 4 B per element of the
+ *    scanned list inside its bounds, plus for each other list 4 B per probe
+ *    through a hub bitmap, or the whole list as a merge consumes it
+ *    (8 + 4·len);
+ *  - a tail level with a single list is counted directly (range size minus
+ *    the matched vertices inside it): 4·(2 + |check|)·⌊log2(len'+1)⌋ with len'
+ *    the list inside the bounds;
+ *  - inclusion–exclusion passes go levels with several lists first, then
+ *    single-list levels (each group in tail order); every pass but the last
+ *    scans, the last one counts directly when its level has a single list.
+ * Returns UINT64_MAX for any other plan shape. */
+static uint32_t flog2p1(uint32_t len) {
+    uint64_t x = (uint64_t)len + 1;
+    uint32_t r = 0;
+    while (x >>= 1) ++r;
+    return r;
+}
+
+uint64_t oracle_alg_bytes_root_leaf(const uint32_t *off, const uint32_t *nb, uint32_t n, const sge_plan_blob *p,
+                                    uint64_t stride, uint64_t offset, uint32_t root_max_degree, uint32_t hub_min) {
+    if (p->num_enum != 2 || p->join_style != SGE_JOIN_WCOJ || p->tail_len == 0 || p->tail_len > SGE_MAX_TAIL)
+        return UINT64_MAX;
+    uint32_t *eu, *ev, maxdeg;
+    const uint64_t m = root_edges(off, nb, n, &eu, &ev, &maxdeg);
+    const uint64_t st = stride > 1 ? stride : 1, o0 = stride > 1 ? offset : 0;
+    const uint64_t nedges = m > o0 ? (m - o0 + st - 1) / st : 0;
+    const uint64_t ntasks = p->root_kind == SGE_ROOT_ANY ? 2 * nedges : nedges;
+    const uint32_t T = p->tail_len;
+    const uint32_t passes = p->tail_mode == SGE_TAIL_IEP ? T : 1;
+    uint32_t ord[SGE_MAX_TAIL], no = 0;
+    for (uint32_t pass = 0; pass < 2; ++pass)  /* several lists first, then one */
+        for (uint32_t t = 0; t < passes; ++t)
+            if ((__builtin_popcount(p->parents[2 + t]) == 1) == (pass == 1)) ord[no++] = t;
+    uint64_t total = 0;
+    for (uint64_t t0 = 0; t0 < ntasks; t0 += 32) {
+        uint32_t cm[32][2], nc = 0;
+        const uint64_t t1 = t0 + 32 < ntasks ? t0 + 32 : ntasks;
+        for (uint64_t t = t0; t < t1; ++t) {
+            uint32_t u, v;
+            if (p->root_kind == SGE_ROOT_ANY) {
+                const uint64_t e = o0 + (t >> 1) * st;
+                u = eu[e]; v = ev[e];
+                if (t & 1) { uint32_t x = u; u = v; v = x; }
+            } else {
+                const uint64_t e = o0 + t * st;
+                u = eu[e]; v = ev[e];
+                if (p->root_kind == SGE_ROOT_DESC) { uint32_t x = u; u = v; v = x; }
+            }
+            if (root_max_degree && (off[u + 1] - off[u] > root_max_degree || off[v + 1] - off[v] > root_max_degree))
+                continue;
+            cm[nc][0] = u; cm[nc][1] = v; ++nc;
+        }
+        for (uint32_t s = 0; s < passes; ++s) {
+            const uint32_t i = 2 + ord[s];
+            const uint32_t par = p->parents[i], nsrc = (uint32_t)__builtin_popcount(par);
+            const int direct = (p->tail_mode != SGE_TAIL_IEP || s + 1 == T) && nsrc == 1;
+            uint32_t slot[2], ns = 0;
+            for (uint32_t j = 0; j < 2; ++j) if ((par >> j) & 1u) slot[ns++] = j;
+            /* each root's lists and bounds */
+            uint32_t len[32][2], trimmed[32][2];
+            for (uint32_t l = 0; l < nc; ++l) {
+                uint32_t lo = 0, hi = 0xFFFFFFFFu;
+                for (uint32_t j = 0; j < 2; ++j) {
+                    if ((p->lower[i] >> j) & 1u) lo = cm[l][j] > lo ? cm[l][j] : lo;
+                    if ((p->upper[i] >> j) & 1u) hi = cm[l][j] < hi ? cm[l][j] : hi;
+                }
+                for (uint32_t q = 0; q < ns; ++q) {
+                    const uint32_t v = cm[l][slot[q]];
+                    const uint32_t *a = nb + off[v];
+                    const uint32_t la = off[v + 1] - off[v];
+                    uint32_t c = 0;
+                    for (uint32_t e = 0; e < la; ++e)
+                        c += (!p->lower[i] || a[e] > lo) && (!p->upper[i] || a[e] < hi);
+                    len[l][q] = la;
+                    trimmed[l][q] = c;
+                }
+            }
+            if (direct) {
+                for (uint32_t l = 0; l < nc; ++l)
+                    total += 4ull * (2u + (uint32_t)__builtin_popcount(p->check[i])) * flog2p1(trimmed[l][0]);
+                continue;
+            }
+            uint32_t bq = 0;
+            unsigned long long best = ~0ull;
+            for (uint32_t q = 0; q < ns; ++q) {
+                unsigned long long cost = 0;
+                for (uint32_t l = 0; l < nc; ++l) {
+                    unsigned long long allp = 0, own = 0;
+                    for (uint32_t r = 0; r < ns; ++r) {
+                        const unsigned long long pc = len[l][r] >= hub_min ? 1u : 2u + flog2p1(len[l][r]);
+                        allp += pc;
+                        if (r == q) own = pc;
+                    }
+                    cost += (unsigned long long)len[l][q] * (allp - own + 1);
+                }
+                if (cost < best) { best = cost; bq = q; }
+            }
+            for (uint32_t l = 0; l < nc; ++l) {
+                const uint64_t blen = trimmed[l][bq];
+                total += 4ull * blen;
+                for (uint32_t q = 0; q < ns; ++q)
+                    if (q != bq) total += len[l][q] >= hub_min ? 4ull * blen : 8ull + 4ull * len[l][q];
+            }
+        }
+    }
+    free(eu);
+    free(ev);
+    return total;
+}

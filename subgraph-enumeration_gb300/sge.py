@@ -418,14 +418,19 @@ def _plan_opts(iep: bool, exploration: bool, max_tail: int, seed: int) -> PlanOp
 
 
 def candidates(pattern: PatternGraph, stats: "GraphStats | None", iep: bool = True, exploration: bool = False,
-               cap: int = 64, max_tail: int = SGE_MAX_TAIL, symmetry_seq=None, root_edge=None) -> list[PlanBlob]:
+               cap: int = 64, max_tail: int = SGE_MAX_TAIL, symmetry_seq=None, root_edge=None,
+               force_order=None) -> list[PlanBlob]:
     """Every executable plan of the pattern, cheapest first by the cost model
-    (symmetry_seq / root_edge as in plan())."""
+    (symmetry_seq / root_edge as in plan(); force_order: only that matching
+    order, with every tail length and restriction scheme)."""
     arr = (PlanBlob * cap)()
     n = u32()
     e = pattern.flat()
     o = _plan_opts(iep, exploration, max_tail, 1)
-    keep = _fix(o, symmetry_seq, root_edge)  # noqa: F841 (kept alive for the call)
+    keep = _fix(o, symmetry_seq, root_edge)  # (kept alive for the call)
+    if force_order is not None:
+        keep.append(np.ascontiguousarray(force_order, dtype=np.uint32))
+        o.force_order = _u32p(keep[-1])
     _check(lib().sge_plan_candidates(pattern.k, pattern.m, _u32p(e), C.byref(stats) if stats is not None else None,
                                      C.byref(o), arr, cap, C.byref(n)))
     return [PlanBlob.from_buffer_copy(arr[i]) for i in range(n.value)]

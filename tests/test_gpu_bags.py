@@ -92,17 +92,29 @@ def test_two_triangles_4cycle_against_the_oracle(sge, oracle, gold_rmat):
         with eng.bags(p, TWO_TRIANGLES_4CYCLE_BAGS) as bg:
             info = bg.info()
             assert info["relations"] == 2 and sorted(info["own_vertices"]) == [0, 5]
-            for iep in (False, True):
-                b, nb = sge.plan_from_reference(p, TWO_TRIANGLES_4CYCLE_BAGS, eng, iep=iep)
-                assert nb == 5
+            imported = [sge.plan_from_reference(p, TWO_TRIANGLES_4CYCLE_BAGS, eng, iep=iep)[0] for iep in (0, 1)]
+            # the imported order with its longest tail: both own vertices (0, 5) are tail levels
+            two = longest_tail(sge, p, eng, imported[1])
+            assert two.tail_len == 2 and sorted(two.order[4:6]) == [0, 5]
+            for b in imported + [two]:
                 full, _, st = eng.count([b], bags=[bg])
-                assert st["bag_levels"] == [2 if iep else 1]
+                tail = set(b.order[b.num_enum:b.k])
+                assert st["bag_levels"] == [len(tail & {0, 5})]
                 assert full == eng.count([b])[0]
                 # a root sample, on the oracle too
                 stride = 64
                 s, _, _ = eng.count([b], bags=[bg], root_stride=stride, root_offset=3)
                 inst, _ = oracle.count_plan(g.offsets, g.nbrs, b, threads=0, stride=stride, offset=3)
                 assert s[0] == inst * b.count_multiplier and s[0] > 0
+
+
+def longest_tail(sge, p, eng, imported):
+    """The imported plan's matching order with its longest tail (the cost
+    model may prefer to enumerate an own vertex of a bag instead)."""
+    c = sge.candidates(p, eng.graph.stats(), cap=64, force_order=list(imported.order[:p.k]))
+    b = max(c, key=lambda x: x.tail_len)
+    b.count_multiplier, b.single_bag, b.choose_wrap = imported.count_multiplier, imported.single_bag, 1
+    return b
 
 
 def test_relation_is_every_embedding_of_the_bag(sge, graphs):
