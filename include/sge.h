@@ -321,7 +321,8 @@ sge_status sge_plan_pattern_sampled(uint32_t k, uint32_t m, const uint32_t *edge
  * for callers that keep the reference's planner: the global bag's order runs
  * first, then each other bag's own attributes in its order (as the trie join
  * of sharedJoin/globalJoin visits them), with this library's symmetry
- * restrictions and leaf counting for that order.  "Number of matches"
+ * restrictions for that order; the own attributes are counted at the leaf
+ * (the longest tail they allow when opts->use_iep, one level otherwise).  "Number of matches"
  * follows the imported plan's shape: embeddings for one bag, instances for
  * several (relation/graph.cpp:910-1077).  The bags must cover every vertex
  * and every edge of the pattern.  stats may be NULL; opts (may be NULL)

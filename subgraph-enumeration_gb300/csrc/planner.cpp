@@ -847,8 +847,20 @@ extern "C" sge_status sge_plan_from_order_text(uint32_t k, uint32_t m, const uin
     o.max_tail = SGE_MAX_TAIL;
     if (opts) o = *opts;
     o.force_order = order;
-    st = sge_plan_pattern_stats(k, m, edges, stats, &o, out);
+    std::vector<Candidate> cands;
+    st = collect_candidates(k, m, edges, stats, &o, cands);
     if (st != SGE_OK) return st;
+    // sharedJoin matches the global bag and counts the other bags' own
+    // attributes at the leaf (join.cpp:1520-1691): the tail is as long as the
+    // attributes outside the global bag allow (cheapest such candidate; the
+    // candidates come sorted by cost)
+    uint32_t outside = k - (uint32_t)__builtin_popcount(bag_mask.back());
+    size_t pick = 0;
+    for (size_t i = 0; i < cands.size(); ++i)
+        if (cands[i].blob.tail_len <= std::max<uint32_t>(outside, 1u) &&
+            cands[i].blob.tail_len > cands[pick].blob.tail_len)
+            pick = i;
+    *out = cands[pick].blob;
     // "Number of matches" follows the imported plan's shape: embeddings for a
     // one-bag plan, instances otherwise (relation/graph.cpp:910-1077,
     // plan/decomposition.cpp:983-986)
