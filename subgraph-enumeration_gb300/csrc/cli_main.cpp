@@ -3,7 +3,11 @@
 //   -q query  -d data  [-r result-log]  [-i] (exploration-style)  [-u] (IEP)
 //   [-t threads]  [--help|-h]
 // plus additive flags: --device N, --batch LIST (one pattern path per line,
-// counted in one persistent launch), --seed S.
+// counted in one persistent launch), --seed S, --plan FILE (run the plan the
+// reference printed: its "num bags:" block or a whole log holding it, imported
+// by sge_plan_from_order_text instead of planning here) and --bags (with
+// --plan: materialise the decomposition's bag relations as tries and let the
+// leaf read them, sge_bags_create + sge_plan_use_bags).
 // Like the reference, -r redirects the text log to a file; it also writes the
 // sorted instance set to <file>.matches (<file>.<i>.matches for --batch), one
 // row per instance in the row format of the reference's storeMatches
@@ -15,6 +19,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <iterator>
 #include <iostream>
 #include <string>
 #include <vector>
@@ -24,8 +29,8 @@
 namespace {
 
 struct Args {
-    std::string q, d, r, batch;
-    bool iep = false, explore = false, help = false;
+    std::string q, d, r, batch, plan;
+    bool iep = false, explore = false, help = false, bags = false;
     int threads = 0, device = 0;
     unsigned long long seed = 1;
 };
@@ -48,6 +53,8 @@ bool parse(int argc, char **argv, Args &a) {
         else if (s == "--device") { if (!need(v)) return false; a.device = atoi(v.c_str()); }
         else if (s == "--batch") { if (!need(a.batch)) return false; }
         else if (s == "--seed") { if (!need(v)) return false; a.seed = strtoull(v.c_str(), nullptr, 10); }
+        else if (s == "--plan") { if (!need(a.plan)) return false; }
+        else if (s == "--bags") a.bags = true;
         else if (s == "-h" || s == "--help") a.help = true;
         else { std::cerr << "unknown option " << s << "\n"; return false; }
     }
@@ -56,7 +63,7 @@ bool parse(int argc, char **argv, Args &a) {
 
 void usage() {
     std::cout << "Usage: graph_mining_system -q QUERY -d DATA [-r RESULT] [-i] [-u] [-t THREADS]\n"
-                 "       [--device N] [--batch PATTERN_LIST] [--seed S]\n"
+                 "       [--device N] [--batch PATTERN_LIST] [--seed S] [--plan REFERENCE_PLAN [--bags]]\n"
                  "  -q  query graph path\n  -d  data graph path (text or BINGRPH)\n"
                  "  -r  result path (log destination)\n  -i  exploration-style intersection\n"
                  "  -u  IEP counting of the last levels\n  -t  threads (accepted; the GPU uses all SMs)\n";
@@ -66,9 +73,16 @@ void usage() {
 
 int main(int argc, char **argv) {
     Args a;
-    if (!parse(argc, argv, a) || a.help || (a.q.empty() && a.batch.empty()) || a.d.empty()) {
+    if (!parse(argc, argv, a) || a.help || (a.q.empty() && a.batch.empty()) || a.d.empty() ||
+        (!a.plan.empty() && !a.batch.empty()) || (a.bags && a.plan.empty())) {
         usage();
         return a.help ? 0 : 1;
+    }
+    std::string plan_text;
+    if (!a.plan.empty()) {
+        std::ifstream pf(a.plan);
+        if (!pf) { std::cout << "Can not open file " << a.plan << "!" << std::endl; return 1; }
+        plan_text.assign(std::istreambuf_iterator<char>(pf), std::istreambuf_iterator<char>());
     }
     std::ofstream file;
     if (!a.r.empty()) file.open(a.r);
@@ -98,6 +112,13 @@ int main(int argc, char **argv) {
     std::vector<sge_plan_blob> blobs;
     std::vector<std::vector<uint32_t>> pedges;
     std::vector<uint32_t> pk;
+    std::vector<uint32_t> nbags;
+    sge_bags *bags = nullptr;
+    sge_graph_stats gst{};
+    if (!plan_text.empty() && sge_graph_stats_compute(off, nb, n, &gst) != SGE_OK) {
+        std::cout << "error: " << sge_last_error() << std::endl;
+        return 1;
+    }
     for (auto &qp : queries) {
         uint32_t k, m, edges[2 * SGE_MAX_K * SGE_MAX_K];
         if (sge_load_pattern_file(qp.c_str(), &k, &m, edges) != SGE_OK) {
@@ -110,7 +131,11 @@ int main(int argc, char **argv) {
         po.max_tail = SGE_MAX_TAIL;
         po.seed = a.seed;
         sge_plan_blob b;
-        if (sge_plan_pattern(k, m, edges, g, &po, &b) != SGE_OK) {
+        uint32_t nb_plan = 0;
+        const sge_status ps = plan_text.empty()
+                                  ? sge_plan_pattern(k, m, edges, g, &po, &b)
+                                  : sge_plan_from_order_text(k, m, edges, plan_text.c_str(), &gst, &po, &b, &nb_plan);
+        if (ps != SGE_OK) {
             std::cout << "error: " << sge_last_error() << std::endl;
             return 1;
         }
@@ -119,6 +144,15 @@ int main(int argc, char **argv) {
             std::cout << "error: " << sge_last_error() << std::endl;
             return 1;
         }
+        if (a.bags) {
+            uint32_t levels = 0;
+            if (sge_bags_create(g, k, m, edges, plan_text.c_str(), 0, &bags) != SGE_OK ||
+                sge_plan_use_bags(p, bags, &levels) != SGE_OK) {
+                std::cout << "error: " << sge_last_error() << std::endl;
+                return 1;
+            }
+        }
+        nbags.push_back(plan_text.empty() ? (b.single_bag ? 1u : 2u) : nb_plan);
         blobs.push_back(b);
         plans.push_back(p);
         pedges.emplace_back(edges, edges + 2 * m);
@@ -127,12 +161,18 @@ int main(int argc, char **argv) {
     double plan_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     for (size_t i = 0; i < blobs.size(); ++i) {
         const sge_plan_blob &b = blobs[i];
-        out << "num bags: " << (b.single_bag ? 1 : 2) << std::endl;
+        out << "num bags: " << nbags[i] << std::endl;
         out << "matching order:";
         for (uint32_t l = 0; l < b.k; ++l) out << (l ? "," : " ") << b.order[l];
         out << std::endl;
     }
     out << "Planning time (s): " << plan_s << std::endl;
+    if (bags) {
+        uint32_t nrel = 0, skipped = 0;
+        uint64_t rows = 0, bytes = 0;
+        sge_bags_info(bags, &nrel, &rows, &bytes, nullptr, &skipped);
+        out << "bag relations: " << nrel << " (" << rows << " tuples, " << bytes << " bytes on the device)" << std::endl;
+    }
     out << "traverse all level: 0" << std::endl;
     out << "use iep: " << (a.iep ? 1 : 0) << std::endl;
     if (a.threads > 1) out << "Number of threads: " << a.threads << std::endl;
@@ -188,6 +228,7 @@ int main(int argc, char **argv) {
         }
     }
     for (auto *p : plans) sge_plan_destroy(p);
+    sge_bags_destroy(bags);
     sge_graph_destroy(g);
     sge_free_host(off);
     sge_free_host(nb);

@@ -64,3 +64,26 @@ def test_cli_result_file_holds_sorted_instance_set(sge, oracle, patterns, graphs
     want = oracle.canonical_instances(oracle.list_embeddings(g.offsets, g.nbrs, p.k, p.edges),
                                       np.array(sge_perms(sge, p)))
     assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("bags", [False, True])
+def test_cli_runs_the_reference_plan(sge, patterns, tmp_path, bags):
+    """--plan takes the decomposition the reference printed (the first
+    three-bag one it printed on ca-netscience in -u mode, inside other log
+    lines) and runs it; --bags materialises its bag relations as tries.  The
+    reference's count either way."""
+    import json
+    rows = json.loads((GOLDEN / "reference_plans.json").read_text())["rows"]
+    r = next(x for x in rows if x["rc"] == 0 and x["count"] and x["mode"] == "u"
+             and x["plan"].startswith("num bags: 3"))
+    q = tmp_path / "q.txt"
+    q.write_text(pattern_of(sge, patterns, r["pattern"]).text())
+    plan = tmp_path / "plan.txt"
+    plan.write_text("some log line\n" + r["plan"] + "Number of matches: (from the reference)\n")
+    cmd = [str(PKG / "_build" / "graph_mining_system"), "-q", str(q), "-d", str(GOLDEN / "ca_netscience.el"), "-u",
+           "--plan", str(plan)] + (["--bags"] if bags else [])
+    out = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert re.search(rf"Number of matches: {r['count']}\b", out.stdout), out.stdout
+    assert "num bags: 3" in out.stdout
+    assert ("bag relations:" in out.stdout) == bags
