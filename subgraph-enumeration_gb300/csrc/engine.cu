@@ -309,9 +309,14 @@ __device__ __forceinline__ unsigned long long choose_leaf(unsigned long long n, 
 }
 
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);
-    return v;
+    // three 32-bit warp reductions (redux.sync) instead of five 64-bit
+    // shuffle steps: the high words (only their sum mod 2^32 matters) and the
+    // low words in 16-bit halves (each half's sum stays below 2^21)
+    const uint32_t lo = (uint32_t)v;
+    const uint32_t hi = __reduce_add_sync(FULL_MASK, (uint32_t)(v >> 32));
+    const uint32_t a = __reduce_add_sync(FULL_MASK, lo >> 16);
+    const uint32_t b = __reduce_add_sync(FULL_MASK, lo & 0xFFFFu);
+    return ((unsigned long long)hi << 32) + ((unsigned long long)a << 16) + b;
 }
 
 // Bounds of level i from the current partial match: keep lo < x < hi.
