@@ -2081,10 +2081,9 @@ sge_status build_hub_index(sge_graph *g, const uint32_t *off) {
     for (uint32_t v = 0; v < n; ++v)
         if (off[v + 1] - off[v] >= thr) { slot[v] = (int32_t)hubs.size(); hubs.push_back(v); }
     uint32_t *d_hubs = nullptr;
-    cudaError_t e;
-    if ((e = cudaMalloc(&g->d_hub_slot, 4ull * n)) != cudaSuccess ||
-        (e = cudaMalloc(&g->d_hub_bits, 4ull * words * hubs.size())) != cudaSuccess ||
-        (e = cudaMalloc(&d_hubs, 4ull * hubs.size())) != cudaSuccess) {
+    if (cudaMalloc(&g->d_hub_slot, 4ull * n) != cudaSuccess ||
+        cudaMalloc(&g->d_hub_bits, 4ull * words * hubs.size()) != cudaSuccess ||
+        cudaMalloc(&d_hubs, 4ull * hubs.size()) != cudaSuccess) {
         cudaFree(g->d_hub_slot);
         cudaFree(g->d_hub_bits);
         g->d_hub_slot = nullptr;
@@ -2129,10 +2128,20 @@ sge_status ensure_batch(sge_graph *g, size_t bytes) {
 // the entries of N(w) below w, which maps the upper entries one-to-one onto
 // lower ones, so with equally many upper and lower entries every lower entry
 // is some upper entry's mirror too.
-sge_status validate_csr(const uint32_t *off, const uint32_t *nbrs, uint32_t n, uint64_t nnz) {
+// Offsets: off[0] = 0, off[n] = nnz, monotone (every list inside the array).
+sge_status validate_offsets(const uint32_t *off, uint32_t n, uint64_t nnz) {
     if (off[0] != 0 || off[n] != nnz) return fail(SGE_BAD_INPUT, "offsets[0] must be 0 and offsets[n] = %llu", (unsigned long long)nnz);
     for (uint32_t v = 0; v < n; ++v)
         if (off[v + 1] < off[v]) return fail(SGE_BAD_INPUT, "offsets not monotone at vertex %u", v);
+    return SGE_OK;
+}
+
+// The lists on the host: strictly increasing, in range, no self-loop, and
+// symmetric (one search per entry above the diagonal, and as many entries
+// above the diagonal as below).
+sge_status validate_csr(const uint32_t *off, const uint32_t *nbrs, uint32_t n, uint64_t nnz) {
+    sge_status ost = validate_offsets(off, n, nnz);
+    if (ost != SGE_OK) return ost;
     unsigned nt = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
     std::atomic<int> bad{0};
     std::atomic<uint32_t> bad_v{0};
@@ -2414,6 +2423,47 @@ sge_status finish_counts(const LaunchCfg &L, const unsigned long long *hc, uint3
 
 }  // namespace
 
+// Directed-entry count above which sge_graph_create checks the lists on the
+// device (the host check of 128M entries takes seconds; the device's, ms).
+constexpr uint64_t SGE_HOST_VALIDATE_MAX = 1ull << 22;
+
+namespace {
+__global__ void csr_check_kernel(const uint32_t *off, const uint32_t *adj, uint32_t n, uint32_t *res,
+                                 unsigned long long *cnt);
+}  // namespace
+
+namespace sge_csr_check {
+// validate_csr's list checks for a CSR already on the device (same messages).
+sge_status validate_csr_device(const uint32_t *d_off, const uint32_t *d_adj, uint32_t n, int device) {
+    uint32_t *res = nullptr;
+    unsigned long long *cnt = nullptr;
+    CUDA_TRY(cudaMalloc(&res, 16));
+    cudaError_t e = cudaMalloc(&cnt, 16);
+    if (e != cudaSuccess) { cudaFree(res); return fail(SGE_OOM, "CSR check: %s", cudaGetErrorString(e)); }
+    const uint32_t init[4] = {0u, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u};
+    uint32_t h[4] = {0, 0, 0, 0};
+    unsigned long long hc[2] = {0, 0};
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    e = cudaMemcpy(res, init, 16, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(cnt, 0, 16);
+    if (e == cudaSuccess) {
+        csr_check_kernel<<<(unsigned)std::max(sms, 1) * 8u, 256>>>(d_off, d_adj, n, res, cnt);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(h, res, 16, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(hc, cnt, 16, cudaMemcpyDeviceToHost);
+    cudaFree(res);
+    cudaFree(cnt);
+    if (e != cudaSuccess) return fail(SGE_CUDA_ERROR, "CSR check: %s", cudaGetErrorString(e));
+    if (h[0] & 2u)
+        return fail(SGE_BAD_INPUT, "neighbour list of vertex %u is not strictly increasing, out of range, or has a self-loop", h[1]);
+    if (h[0] & 4u) return fail(SGE_BAD_INPUT, "CSR is not symmetric at vertex %u", h[2]);
+    if (hc[0] != hc[1]) return fail(SGE_BAD_INPUT, "CSR is not symmetric at vertex %u", 0u);
+    return SGE_OK;
+}
+}  // namespace sge_csr_check
+
 extern "C" {
 
 const char *sge_version(void) { return "sge 0.1 (sm_103a, ABI 1)"; }
@@ -2426,10 +2476,14 @@ int sge_device_count(void) {
 
 sge_status sge_graph_create(const uint32_t *offsets, const uint32_t *nbrs, uint32_t n, uint64_t nnz, int device,
                             sge_graph **out) {
+    using sge_csr_check::validate_csr_device;
     if (!offsets || (!nbrs && nnz) || !out) return fail(SGE_BAD_INPUT, "sge_graph_create: null argument");
     if (nnz % 2) return fail(SGE_BAD_INPUT, "odd number of directed edges (%llu)", (unsigned long long)nnz);
     if (nnz >= (1ull << 32)) return fail(SGE_BAD_INPUT, "%llu directed edges exceed the uint32 EdgeID range", (unsigned long long)nnz);
-    sge_status st = validate_csr(offsets, nbrs, n, nnz);
+    // small graphs are checked on the host before any device is touched;
+    // large ones have their offsets checked here and their lists on the device
+    const bool on_device = nnz > SGE_HOST_VALIDATE_MAX;
+    sge_status st = on_device ? validate_offsets(offsets, n, nnz) : validate_csr(offsets, nbrs, n, nnz);
     if (st != SGE_OK) return st;
     int ndev = sge_device_count();
     if (ndev == 0) return fail(SGE_NO_DEVICE, "no CUDA device visible");
@@ -2451,12 +2505,56 @@ sge_status sge_graph_create(const uint32_t *offsets, const uint32_t *nbrs, uint3
         cudaFree(d_adj);
         return fail(SGE_CUDA_ERROR, "graph upload failed: %s", cudaGetErrorString(e));
     }
+    if (on_device) {
+        st = validate_csr_device(d_off, d_adj, n, device);
+        if (st != SGE_OK) {
+            cudaFree(d_off);
+            cudaFree(d_adj);
+            return st;
+        }
+    }
     return graph_adopt(d_off, d_adj, n, nnz, device, out, offsets, nbrs);
 }
 
 }  // extern "C"
 
 namespace {
+// The checks of validate_csr on the device, one warp per vertex: res[0] |= 2
+// (a list not strictly increasing, out of range or with a self-loop; res[1] =
+// the smallest such vertex) or 4 (an entry above the diagonal without its
+// reverse; res[2] = the smallest such vertex); cnt[0/1] = entries above/below
+// the diagonal.  Offsets were checked on the host, so every list is in bounds.
+__global__ void csr_check_kernel(const uint32_t *off, const uint32_t *adj, uint32_t n, uint32_t *res,
+                                 unsigned long long *cnt) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    unsigned long long up = 0, lo = 0;
+    for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += nw) {
+        const uint32_t a = off[v], b = off[v + 1];
+        for (uint32_t e = a + lane; e < b; e += 32) {
+            const uint32_t w = adj[e];
+            if (w >= n || w == v || (e > a && adj[e - 1] >= w)) {
+                atomicOr(res, 2u);
+                atomicMin(res + 1, v);
+                continue;
+            }
+            if (w < v) { ++lo; continue; }
+            ++up;
+            const uint32_t wa = off[w];
+            if (!contains(adj + wa, off[w + 1] - wa, v)) {
+                atomicOr(res, 4u);
+                atomicMin(res + 2, v);
+            }
+        }
+    }
+    up = warp_sum_u64(up);
+    lo = warp_sum_u64(lo);
+    if (lane == 0) {
+        atomicAdd(cnt, up);
+        atomicAdd(cnt + 1, lo);
+    }
+}
+
 // Root edges of a device CSR: directed edge e = (src(e), adj[e]) is a root
 // when adj[e] > src(e); pos[e] is its rank among the roots (CSR order).
 __global__ void root_flags_kernel(const uint32_t *off, const uint32_t *adj, uint32_t n, unsigned long long nnz,

@@ -78,3 +78,31 @@ def test_empty_and_bad_edge_lists(sge):
     with pytest.raises(sge.SgeError):
         sge.Engine.rmat_device(4, 1000, seed=1)  # too dense for 16 vertices
 
+
+
+def test_large_host_csr_is_checked_on_the_device(sge):
+    """Above 2^22 directed entries sge_graph_create checks the lists on the
+    device (the offsets still on the host): the same errors as the host check."""
+    import ctypes as C
+    g = sge.gen_rmat(18, 3_000_000, seed=2)
+    off, nb = g.offsets.copy(), g.nbrs.copy()
+    assert nb.size > (1 << 22)
+    with sge.Engine(g) as eng:
+        assert eng.info()["num_directed_edges"] == nb.size
+    deg = np.diff(off)
+    v = int(np.argmax(deg > 8))  # a vertex with a list long enough to edit in place
+    a = int(off[v])
+    lst = nb[a:a + int(deg[v])]
+    gap = int(np.argmax(np.diff(lst.astype(np.int64)) > 1))  # two entries with room between them
+    cases = {}
+    bad = nb.copy(); bad[a + gap], bad[a + gap + 1] = bad[a + gap + 1], bad[a + gap]
+    cases["strictly increasing"] = bad                      # two entries swapped
+    bad = nb.copy(); bad[a + gap] = lst[gap] + 1
+    cases["not symmetric"] = bad                            # an entry with no reverse entry
+    bad = nb.copy(); bad[-1] = g.num_vertices
+    cases["out of range"] = bad                             # the last list's last entry past n
+    for want, arr in cases.items():
+        h = C.c_void_p()
+        st = sge.lib().sge_graph_create(sge._u32p(off), sge._u32p(arr), g.num_vertices, arr.size, 0, C.byref(h))
+        assert sge.STATUS[st] == "BAD_INPUT", want
+        assert want in sge.lib().sge_last_error().decode(), (want, sge.lib().sge_last_error())
