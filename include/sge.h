@@ -136,7 +136,11 @@ typedef struct sge_plan_blob {
      * reference's even where it wraps.  Either way a product that reaches
      * 2^64 sets bit 2 of sge_stats.status_flags. */
     uint32_t choose_wrap;
-    uint32_t reserved;
+    /* 1: planned for vertex labels (sge_plan_opts.vertex_labels): symmetry
+     * restrictions from label-preserving automorphisms only, count_multiplier
+     * = their number; sge_plan_set_labels must attach the same labels to the
+     * plan and sge_graph_set_labels the data graph's before counting. */
+    uint32_t labeled;
 } sge_plan_blob;
 
 /* Planner options */
@@ -155,6 +159,10 @@ typedef struct sge_plan_opts {
     /* optional: 2 adjacent pattern vertices every candidate order starts
      * with, in either orientation */
     const uint32_t *root_edge;
+    /* optional: k pattern vertex labels (labeled matching: a pattern vertex
+     * maps only to data vertices with its label; the reference's LabeledGraph
+     * and candidate space, relation/candidate_space.cpp:112-760) */
+    const uint32_t *vertex_labels;
 } sge_plan_opts;
 
 /* Execution options */
@@ -228,6 +236,13 @@ sge_status sge_load_graph_file(const char *path, uint32_t **offsets, uint32_t **
 sge_status sge_save_graph_binary(const char *path, const uint32_t *offsets, const uint32_t *nbrs,
                                  uint32_t num_vertices);
 sge_status sge_load_pattern_file(const char *path, uint32_t *k, uint32_t *m, uint32_t *edges /* 2*m, cap 2*SGE_MAX_K*SGE_MAX_K */);
+/* Labeled graph in the reference's text format (LabeledGraph::loadLabeldGraphFromText,
+ * relation/labeled_graph.cpp:63-143): "t n m", then "v id label degree" per
+ * vertex and "e u v" per undirected edge.  Returns the symmetric CSR with
+ * lists sorted by id (as sge_load_graph_file) and one label per vertex; all
+ * three arrays are malloc'ed (sge_free_host).  Degrees must match the edges. */
+sge_status sge_load_labeled_graph_file(const char *path, uint32_t **offsets, uint32_t **nbrs, uint32_t **labels,
+                                       uint32_t *num_vertices, uint64_t *num_directed_edges);
 /* CSR from an undirected edge list (u,v pairs): symmetric, per-list sorted
  * (Graph::addDirectedEdges, graph.cpp:143-173).  dedup!=0 also removes
  * duplicates and self-loops (the reference does not; its inputs must be clean). */
@@ -376,6 +391,16 @@ typedef struct sge_plan_tuning {
     uint32_t no_hub_bitmaps;    /* 1: this plan probes adjacency lists by binary search only */
 } sge_plan_tuning;
 sge_status sge_plan_set_tuning(sge_plan *p, const sge_plan_tuning *t);
+/* Labeled matching.  sge_graph_set_labels uploads one label per data vertex
+ * (n values; NULL removes them); sge_plan_set_labels attaches k pattern
+ * labels (pattern vertex order; NULL detaches) to a plan planned with the
+ * same labels (blob.labeled).  A labeled plan then matches pattern vertex u
+ * only to data vertices of label labels[u]: the root edge's ends and every
+ * enumerated candidate are checked, and tail levels are counted by a scan
+ * that checks labels (not by range size).  WCOJ plans only; bag relations,
+ * sge_enumerate and sge_count_noalloc take unlabeled plans. */
+sge_status sge_graph_set_labels(sge_graph *g, const uint32_t *labels);
+sge_status sge_plan_set_labels(sge_plan *p, const uint32_t *labels);
 
 /* ---- execution (replaces sharedJoin / parSharedJoin) ----
  * Counts nplans patterns over g in one persistent launch (the batch shares

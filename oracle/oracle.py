@@ -64,6 +64,11 @@ def lib() -> C.CDLL:
         L.oracle_csr_from_sorted_edges.argtypes = [_P(u32), u64, u32, _P(u32), _P(u32)]
         L.oracle_free.restype = None
         L.oracle_free.argtypes = [C.c_void_p]
+        L.oracle_aut_size_labeled.restype = u64
+        L.oracle_aut_size_labeled.argtypes = [u32, u32, _P(u32), _P(u32)]
+        L.oracle_bruteforce_embeddings_labeled.restype = u64
+        L.oracle_bruteforce_embeddings_labeled.argtypes = [_P(u32), _P(u32), u32, u32, u32, _P(u32), _P(u32), _P(u32),
+                                                          C.c_int]
         L.oracle_alg_bytes_root_leaf.restype = u64
         L.oracle_alg_bytes_root_leaf.argtypes = [_P(u32), _P(u32), u32, C.c_void_p, u64, u64, u32, u32]
         _lib = L
@@ -258,3 +263,22 @@ def alg_bytes_root_leaf(offsets, nbrs, blob, stride: int = 1, offset: int = 0, r
     if r == (1 << 64) - 1:
         raise ValueError("alg_bytes_root_leaf needs a WCOJ plan with two enumerated levels")
     return int(r)
+
+
+def aut_size_labeled(k: int, edges, labels) -> int:
+    """Automorphisms that preserve adjacency and the vertex labels."""
+    e = np.ascontiguousarray(np.asarray(edges, np.uint32).reshape(-1))
+    lab = np.ascontiguousarray(labels, np.uint32)
+    return int(lib().oracle_aut_size_labeled(k, e.size // 2, _p(e), _p(lab)))
+
+
+def bruteforce_embeddings_labeled(offsets, nbrs, k: int, edges, pattern_labels, graph_labels,
+                                  threads: int = 0) -> int:
+    """Embeddings of a labeled pattern (pattern vertex u onto vertices of label
+    pattern_labels[u] only), by brute-force DFS."""
+    off, nb = _arr(offsets), _arr(nbrs)
+    e = np.ascontiguousarray(np.asarray(edges, np.uint32).reshape(-1))
+    pl = np.ascontiguousarray(pattern_labels, np.uint32)
+    gl = np.ascontiguousarray(graph_labels, np.uint32)
+    return int(lib().oracle_bruteforce_embeddings_labeled(_p(off), _p(nb), off.size - 1, k, e.size // 2, _p(e), _p(pl),
+                                                          _p(gl), threads))

@@ -260,6 +260,31 @@ uint64_t oracle_aut_size(uint32_t k, uint32_t m, const uint32_t *edges) {
     return cnt;
 }
 
+/* As oracle_aut_size, counting only permutations that also preserve the
+ * vertex labels lab (NULL: unlabeled). */
+uint64_t oracle_aut_size_labeled(uint32_t k, uint32_t m, const uint32_t *edges, const uint32_t *lab) {
+    uint32_t adj[32] = {0};
+    for (uint32_t i = 0; i < m; ++i) { adj[edges[2 * i]] |= 1u << edges[2 * i + 1]; adj[edges[2 * i + 1]] |= 1u << edges[2 * i]; }
+    uint32_t map[32], used = 0, next[33];
+    uint64_t cnt = 0;
+    int i = 0;
+    next[0] = 0;
+    while (i >= 0) {
+        if (i == (int)k) { ++cnt; --i; if (i >= 0) used &= ~(1u << map[i]); continue; }
+        int placed = 0;
+        for (uint32_t c = next[i]; c < k; ++c) {
+            if ((used >> c) & 1u) continue;
+            if (lab && lab[c] != lab[i]) continue;
+            int ok = 1;
+            for (int j = 0; j < i && ok; ++j) if (pat_edge(adj, (uint32_t)i, (uint32_t)j) != pat_edge(adj, c, map[j])) ok = 0;
+            if (!ok) continue;
+            map[i] = c; used |= 1u << c; next[i] = c + 1; ++i; if (i < (int)k) next[i] = 0; placed = 1; break;
+        }
+        if (!placed) { --i; if (i >= 0) used &= ~(1u << map[i]); }
+    }
+    return cnt;
+}
+
 static int has_edge(const uint32_t *off, const uint32_t *nb, uint32_t u, uint32_t v) {
     uint32_t a = off[u], b = off[u + 1];
     return check_exists(nb, a, b, v) != b;
@@ -268,8 +293,19 @@ static int has_edge(const uint32_t *off, const uint32_t *nb, uint32_t u, uint32_
 /* Injective homomorphisms (embeddings) of a connected pattern, by DFS over a
  * connected order; each new vertex ranges over the neighbours of its first
  * earlier neighbour and is checked against all other earlier neighbours. */
+uint64_t oracle_bruteforce_embeddings_labeled(const uint32_t *off, const uint32_t *nb, uint32_t n, uint32_t k,
+                                              uint32_t m, const uint32_t *edges, const uint32_t *plab,
+                                              const uint32_t *glab, int threads);
 uint64_t oracle_bruteforce_embeddings(const uint32_t *off, const uint32_t *nb, uint32_t n, uint32_t k, uint32_t m,
                                       const uint32_t *edges, int threads) {
+    return oracle_bruteforce_embeddings_labeled(off, nb, n, k, m, edges, NULL, NULL, threads);
+}
+
+/* Embeddings of a labeled pattern: pattern vertex u maps only to data vertices
+ * v with glab[v] == plab[u] (both NULL: unlabeled). */
+uint64_t oracle_bruteforce_embeddings_labeled(const uint32_t *off, const uint32_t *nb, uint32_t n, uint32_t k,
+                                              uint32_t m, const uint32_t *edges, const uint32_t *plab,
+                                              const uint32_t *glab, int threads) {
     uint32_t adj[32] = {0};
     for (uint32_t i = 0; i < m; ++i) { adj[edges[2 * i]] |= 1u << edges[2 * i + 1]; adj[edges[2 * i + 1]] |= 1u << edges[2 * i]; }
     uint32_t order[32], pos[32], seen = 0;
@@ -304,6 +340,7 @@ uint64_t oracle_bruteforce_embeddings(const uint32_t *off, const uint32_t *nb, u
         uint32_t mm[32], it[32];
         int lv = 0;
         mm[0] = (uint32_t)r;
+        if (plab && glab[r] != plab[order[0]]) continue;
         if (k == 1) { total += 1; continue; }
         lv = 1;
         it[1] = off[mm[first[1]]];
@@ -311,7 +348,7 @@ uint64_t oracle_bruteforce_embeddings(const uint32_t *off, const uint32_t *nb, u
             uint32_t p = mm[first[lv]];
             if (it[lv] >= off[p + 1]) { --lv; continue; }
             uint32_t x = nb[it[lv]++];
-            int ok = 1;
+            int ok = !plab || glab[x] == plab[order[lv]];
             for (int j = 0; j < lv && ok; ++j) if (mm[j] == x) ok = 0;
             for (uint32_t msk = back[lv] & ~(1u << first[lv]); msk && ok; msk &= msk - 1)
                 if (!has_edge(off, nb, mm[__builtin_ctz(msk)], x)) ok = 0;

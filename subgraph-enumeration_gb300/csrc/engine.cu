@@ -139,6 +139,10 @@ struct DevPlan {
     uint8_t trel[2];                              // relation of slot j in `tries`
     uint8_t tkey[2][3];                           // key levels of slot j, in the trie's key order
     uint8_t ntrie, pad2_[3];
+    // labeled matching (sge_plan_set_labels): vlab = the data graph's vertex
+    // labels (null: unlabeled), lab[i] = the label of level i's pattern vertex
+    const uint32_t *vlab;
+    uint32_t lab[SGE_MAX_K];
 };
 static_assert(sizeof(DevPlan) % 4 == 0, "DevPlan is copied as 32-bit words");
 
@@ -173,9 +177,10 @@ struct WarpState {
 // candidate level, and which slots add bounds or exclusions.
 struct TailDesc {
     const uint32_t *ptr[SGE_MAX_K];
+    const uint32_t *vlab;     // labeled plans: the data graph's labels (null: unlabeled)
     uint32_t len[SGE_MAX_K];
     uint32_t exv[SGE_MAX_K];
-    uint32_t lo, hi;
+    uint32_t lo, hi, lab;     // lab: the level's pattern label
     uint8_t kind[SGE_MAX_K];  // 0..2 pinned table; 3 sorted list; 4/5 CSR list of slot 0/1
     int8_t lvl[SGE_MAX_K];    // kind 3: the matched level whose CSR list it is, -1 = a stored list
     uint8_t nsrc, nex, has_lo, has_hi, lo_slots, hi_slots, ex_slots, pad;
@@ -339,6 +344,13 @@ __device__ __forceinline__ bool excluded(const DevPlan &P, const WarpState &W, u
     bool ex = false;
     for (uint32_t msk = P.check[i]; msk; msk &= msk - 1) ex |= (W.m[__ffs(msk) - 1] == x);
     return ex;
+}
+// x may not be level i's match: an earlier match (injectivity) or, for a
+// labeled plan, a vertex of another label.  (Stored lists are filtered by
+// excluded() alone: a later level with another label may reuse them.)
+__device__ __forceinline__ bool rejected(const DevPlan &P, const WarpState &W, uint32_t i, uint32_t x) {
+    if (P.vlab && __ldg(P.vlab + x) != P.lab[i]) return true;
+    return excluded(P, W, i, x);
 }
 
 __device__ __forceinline__ void nbr(const DevGraph &g, uint32_t v, const uint32_t *&p, uint32_t &len) {
@@ -848,6 +860,7 @@ __device__ __forceinline__ uint32_t td_probe_cost(const TailDesc &D, const LeafS
 }
 
 __device__ __forceinline__ bool td_excluded(const TailDesc &D, const LeafState &L, uint32_t l, uint32_t y) {
+    if (D.vlab && __ldg(D.vlab + y) != D.lab) return true;
     bool ex = false;
     for (uint32_t e = 0; e < D.nex; ++e) ex |= D.exv[e] == y;
     if (D.ex_slots & 1u) ex |= L.cm[l][0] == y;
@@ -894,6 +907,8 @@ __device__ void tail_desc(const DevPlan &P, const WarpState &W, const LeafState 
         return true;
     });
     D.nsrc = (uint8_t)n;
+    D.vlab = P.vlab;
+    D.lab = P.lab[i];
     D.has_lo = P.lower[i] != 0;
     D.has_hi = P.upper[i] != 0;
     uint32_t lo = 0, hi = 0xFFFFFFFFu, los = 0, his = 0, exs = 0, nex = 0;
@@ -958,7 +973,7 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
         // scan: range size minus the matched vertices inside it (numResults)
         // (the last inclusion–exclusion pass probes no other tail level, so it
         // is a plain count too)
-        const bool direct = (P.tail_mode != SGE_TAIL_IEP || t + 1 == T) && D.nsrc == 1;
+        const bool direct = (P.tail_mode != SGE_TAIL_IEP || t + 1 == T) && D.nsrc == 1 && !P.vlab;
         if (direct) {
             if (lane < ncand) {
                 const uint32_t *fp = td_ptr(D, L, 0, lane);
@@ -1250,7 +1265,7 @@ __device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32
         const uint32_t idx = b0 + lane;
         bool valid = idx < n;
         const uint32_t xv = valid ? lst[idx] : 0u;
-        if (valid) valid = !excluded(P, W, a, xv);
+        if (valid) valid = !rejected(P, W, a, xv);
         const uint32_t bal = __ballot_sync(FULL_MASK, valid);
         const uint32_t nc = __popc(bal);
         if (valid) S.x[__popc(bal & ((1u << lane) - 1u))] = xv;
@@ -1482,7 +1497,7 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
                 const uint32_t idx = b0 + lane;
                 bool valid = idx < n;
                 const uint32_t x = valid ? lst[idx] : 0u;
-                if (valid) valid = !excluded(P, W, lv, x);
+                if (valid) valid = !rejected(P, W, lv, x);
                 const uint32_t bal = __ballot_sync(FULL_MASK, valid);
                 const uint32_t nc = __popc(bal);
                 if (valid) {
@@ -1509,7 +1524,7 @@ __device__ unsigned long long run_root(const DevPlan &P, WarpState &W, Ctx<STATS
         __syncwarp();
         if (lane == 0) W.pos[lv] = pos + 1;
         __syncwarp();
-        if (excluded(P, W, lv, x)) continue;
+        if (rejected(P, W, lv, x)) continue;
         set_match(c.g, W, lv, x);
         if (STATS) c.partial += 1;
         if (explore && !explore_update(P, W, c, lv)) continue;
@@ -1599,6 +1614,7 @@ __device__ __forceinline__ uint2 root_edge(const DevGraph &g, const DevPlan &P, 
 
 // A root kept by the degree cap: both endpoints of degree <= root_maxdeg.
 __device__ __forceinline__ bool root_kept(const DevGraph &g, const DevPlan &P, uint2 e) {
+    if (P.vlab && (__ldg(P.vlab + e.x) != P.lab[0] || __ldg(P.vlab + e.y) != P.lab[1])) return false;
     if (!P.root_maxdeg) return true;
     return __ldg(g.off + e.x + 1) - __ldg(g.off + e.x) <= P.root_maxdeg &&
            __ldg(g.off + e.y + 1) - __ldg(g.off + e.y) <= P.root_maxdeg;
@@ -1904,6 +1920,7 @@ struct sge_graph {
     int32_t *d_hub_slot = nullptr;
     uint32_t hub_words = 0, hub_min = 0xFFFFFFFFu, hub_count = 0;
     uint64_t hub_bytes = 0;
+    uint32_t *d_labels = nullptr;  // vertex labels (sge_graph_set_labels)
 };
 
 namespace {
@@ -1942,6 +1959,8 @@ struct sge_plan {
     DevPlan dp;
     sge_plan_tuning tune{};
     const sge_bags *bags = nullptr;  // bag relations its tail levels read (sge_plan_use_bags)
+    bool has_labels = false;         // pattern labels attached (sge_plan_set_labels)
+    uint32_t labels[SGE_MAX_K] = {};
 };
 
 namespace sge {
@@ -2019,8 +2038,10 @@ void to_devplan(const sge_plan_blob &b, DevPlan &d) {
     for (uint32_t i = 0; i < SGE_MAX_K; ++i) d.hoist_at[i] = xs.hoist_at[i];
     d.tail_par = 0;
     for (uint32_t i = b.num_enum; i < b.k; ++i) d.tail_par |= b.parents[i];
-    d.pair = xs.pair ? 1u : 0u;
-    d.pair_direct = xs.pair_direct ? 1u : 0u;
+    // (labeled plans check every candidate's label where it is taken, so
+    // they keep the level-by-level DFS: no pair step)
+    d.pair = xs.pair && !b.labeled ? 1u : 0u;
+    d.pair_direct = xs.pair_direct && !b.labeled ? 1u : 0u;
     // exploration: the running list of a tail level whose parents below the
     // leaf are exactly levels 0 and 1 is final once the root is matched;
     // it is pinned in the third table
@@ -2245,6 +2266,12 @@ sge_status prepare_launch(sge_graph *g, const sge_plan *const *plans, uint32_t n
         L.ntr = std::max<uint32_t>(L.ntr, d.ntrie);
         if (plans[i]->bags && plans[i]->bags->g != g)
             return fail(SGE_BAD_INPUT, "plan %u uses bag relations built on another graph", i);
+        if (plans[i]->blob.labeled) {
+            if (!plans[i]->has_labels) return fail(SGE_BAD_INPUT, "plan %u is labeled but has no labels (sge_plan_set_labels)", i);
+            if (!g->d_labels) return fail(SGE_BAD_INPUT, "plan %u is labeled but the graph has no labels (sge_graph_set_labels)", i);
+            d.vlab = g->d_labels;
+            for (uint32_t l = 0; l < d.k; ++l) d.lab[l] = plans[i]->labels[plans[i]->blob.order[l]];
+        }
         if (d.k > SGE_MAX_K) return fail(SGE_UNSUPPORTED, "plan %u has k=%u", i, d.k);
     }
     // pinned-list tables: a bitmap over all vertices when it fits in 4 KB.
@@ -2652,6 +2679,7 @@ sge_status sge_graph_destroy(sge_graph *g) {
     cudaFree(g->d_batch);
     cudaFree(g->d_hub_bits);
     cudaFree(g->d_hub_slot);
+    cudaFree(g->d_labels);
     if (g->ev0) cudaEventDestroy(g->ev0);
     if (g->ev1) cudaEventDestroy(g->ev1);
     if (g->stream) cudaStreamDestroy(g->stream);
@@ -2690,6 +2718,32 @@ sge_status sge_plan_set_tuning(sge_plan *p, const sge_plan_tuning *t) {
     if (!p) return fail(SGE_BAD_INPUT, "sge_plan_set_tuning: null plan");
     if (t) p->tune = *t;
     else p->tune = sge_plan_tuning{};
+    return SGE_OK;
+}
+
+sge_status sge_plan_set_labels(sge_plan *p, const uint32_t *labels) {
+    if (!p) return fail(SGE_BAD_INPUT, "sge_plan_set_labels: null plan");
+    if (!labels) {
+        p->has_labels = false;
+        return SGE_OK;
+    }
+    if (!p->blob.labeled) return fail(SGE_BAD_INPUT, "the plan was planned without labels (sge_plan_opts.vertex_labels)");
+    for (uint32_t u = 0; u < p->blob.k; ++u) p->labels[u] = labels[u];
+    p->has_labels = true;
+    return SGE_OK;
+}
+
+sge_status sge_graph_set_labels(sge_graph *g, const uint32_t *labels) {
+    if (!g) return fail(SGE_BAD_INPUT, "sge_graph_set_labels: null graph");
+    DeviceGuard restore_device;
+    CUDA_TRY(cudaSetDevice(g->device));
+    if (!labels) {
+        cudaFree(g->d_labels);
+        g->d_labels = nullptr;
+        return SGE_OK;
+    }
+    if (!g->d_labels) CUDA_TRY(cudaMalloc(&g->d_labels, 4ull * std::max<uint32_t>(g->n, 1)));
+    CUDA_TRY(cudaMemcpy(g->d_labels, labels, 4ull * g->n, cudaMemcpyHostToDevice));
     return SGE_OK;
 }
 
@@ -2754,6 +2808,7 @@ sge_status sge_plan_pattern_sampled(uint32_t k, uint32_t m, const uint32_t *edge
                                     const sge_plan_opts *opts, uint32_t shortlist, uint64_t sample_stride,
                                     sge_plan_blob *out, double *sampled_ms) {
     if (!g || !out || !edges) return fail(SGE_BAD_INPUT, "sge_plan_pattern_sampled: null argument");
+    if (opts && opts->vertex_labels) return fail(SGE_UNSUPPORTED, "sampled planning takes unlabeled patterns");
     if (shortlist == 0) shortlist = 8;
     std::vector<sge_plan_blob> cands(shortlist);
     uint32_t n = 0;
@@ -2884,6 +2939,7 @@ sge_status sge_enumerate(sge_graph *g, const sge_plan *p, uint32_t *d_out, uint6
     if (!g || !p || !n_matches || (!d_out && capacity)) return fail(SGE_BAD_INPUT, "sge_enumerate: null argument");
     if (p->blob.tail_len != 1)
         return fail(SGE_BAD_INPUT, "sge_enumerate needs a plan with a one-level tail (plan it without IEP)");
+    if (p->blob.labeled) return fail(SGE_UNSUPPORTED, "sge_enumerate takes unlabeled plans");
     DeviceGuard restore_device;
     CUDA_TRY(cudaSetDevice(g->device));
     DevPlan d = p->dp;
@@ -2936,6 +2992,8 @@ sge_status sge_count_host(const uint32_t *offsets, const uint32_t *nbrs, uint32_
                           const sge_plan_blob *blobs, uint32_t nplans, const sge_count_opts *opts, uint64_t *counts,
                           sge_stats *stats) {
     if (!blobs && nplans) return fail(SGE_BAD_INPUT, "sge_count_host: null plans");
+    for (uint32_t i = 0; i < nplans; ++i)
+        if (blobs[i].labeled) return fail(SGE_UNSUPPORTED, "sge_count_host takes unlabeled plans");
     sge_graph *g = nullptr;
     sge_status st = sge_graph_create(offsets, nbrs, n, nnz, 0, &g);
     if (st != SGE_OK) return st;
@@ -3064,6 +3122,7 @@ extern "C" sge_status sge_count_noalloc(const uint32_t *d_offsets, const uint32_
     for (uint32_t i = 0; i < nplans; ++i) {
         sge_status st = sge_plan_validate(&plans[i]);
         if (st != SGE_OK) return st;
+        if (plans[i].labeled) return fail(SGE_UNSUPPORTED, "sge_count_noalloc takes unlabeled plans");
         DevPlan &dp = dps[i];
         to_devplan(plans[i], dp);
         dp.task_begin = 0;
@@ -3327,6 +3386,7 @@ sge_status sge_plan_use_bags(sge_plan *p, const sge_bags *b, uint32_t *levels) {
     const sge_plan_blob &bl = p->blob;
     if (b->k != bl.k) return fail(SGE_BAD_INPUT, "bags of a %u-vertex pattern, plan of %u vertices", b->k, bl.k);
     if (bl.join_style != SGE_JOIN_WCOJ) return fail(SGE_UNSUPPORTED, "bag relations need a WCOJ plan");
+    if (bl.labeled) return fail(SGE_UNSUPPORTED, "bag relations take unlabeled plans");
     uint32_t level_of[SGE_MAX_K];
     for (uint32_t i = 0; i < bl.k; ++i) level_of[bl.order[i]] = i;
     DevPlan &d = p->dp;

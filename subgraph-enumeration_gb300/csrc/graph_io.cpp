@@ -197,6 +197,84 @@ sge_status sge_load_graph_file(const char *path, uint32_t **offsets, uint32_t **
     return build_csr(edges.data(), m, n, 0, offsets, nbrs, nnz);
 }
 
+// "t n m", then "v id label degree" and "e u v" lines in any order
+// (LabeledGraph::loadLabeldGraphFromText, relation/labeled_graph.cpp:63-143).
+// The lists come out sorted by id (the reference sorts by (label, id); the
+// executor keeps id order and checks labels itself).
+sge_status sge_load_labeled_graph_file(const char *path, uint32_t **offsets, uint32_t **nbrs, uint32_t **labels,
+                                       uint32_t *num_vertices, uint64_t *nnz) {
+    if (!path || !offsets || !nbrs || !labels || !num_vertices || !nnz)
+        return fail(SGE_BAD_INPUT, "sge_load_labeled_graph_file: null argument");
+    FileBuf fb(path);
+    if (!fb.ok) return fail(SGE_IO_ERROR, "Can not open file %s .", path);
+    const char *q = fb.data.data(), *end = q + fb.data.size() - 1;
+    auto tag = [&](char &c) {
+        while (q < end && (*q == ' ' || *q == '\t' || *q == '\n' || *q == '\r')) ++q;
+        if (q >= end) return false;
+        c = *q++;
+        return true;
+    };
+    Tok t{q, end};
+    char c = 0;
+    uint64_t n = 0, m = 0;
+    if (!tag(c) || c != 't') return fail(SGE_IO_ERROR, "%s: expected a 't n m' header", path);
+    t.p = q;
+    if (!t.next(n) || !t.next(m)) return fail(SGE_IO_ERROR, "%s: expected a 't n m' header", path);
+    if (n >= (1ull << 32)) return fail(SGE_BAD_INPUT, "%s: %llu vertices", path, (unsigned long long)n);
+    q = t.p;
+    std::vector<uint32_t> lab(n, 0), edges;
+    std::vector<uint64_t> deg(n, 0);
+    std::vector<char> seen(n, 0);
+    edges.reserve(2 * m);
+    while (tag(c)) {
+        t.p = q;
+        if (c == 'v') {
+            uint64_t id, l, d;
+            if (!t.next(id) || !t.next(l) || !t.next(d) || id >= n || l >= (1ull << 32))
+                return fail(SGE_IO_ERROR, "%s: bad vertex line", path);
+            lab[id] = (uint32_t)l;
+            deg[id] = d;
+            seen[id] = 1;
+        } else if (c == 'e') {
+            uint64_t a, b;
+            if (!t.next(a) || !t.next(b) || a >= n || b >= n) return fail(SGE_IO_ERROR, "%s: bad edge line", path);
+            edges.push_back((uint32_t)a);
+            edges.push_back((uint32_t)b);
+        } else {
+            return fail(SGE_IO_ERROR, "%s: unexpected line type '%c'", path, c);
+        }
+        q = t.p;
+    }
+    if (edges.size() / 2 != m)
+        return fail(SGE_IO_ERROR, "error: expecting %llu edges, getting %llu edges.", (unsigned long long)m,
+                    (unsigned long long)(edges.size() / 2));
+    for (uint64_t v = 0; v < n; ++v)
+        if (!seen[v]) return fail(SGE_IO_ERROR, "%s: vertex %llu has no 'v' line", path, (unsigned long long)v);
+    sge_status st = build_csr(edges.data(), m, (uint32_t)n, 0, offsets, nbrs, nnz);
+    if (st != SGE_OK) return st;
+    auto drop = [&]() {
+        free(*offsets);
+        free(*nbrs);
+        *offsets = *nbrs = nullptr;
+    };
+    for (uint64_t v = 0; v < n; ++v) {
+        const uint32_t have = (*offsets)[v + 1] - (*offsets)[v];
+        if (have != deg[v]) {
+            drop();
+            return fail(SGE_IO_ERROR, "%s: vertex %llu declares degree %llu but has %u edges", path,
+                        (unsigned long long)v, (unsigned long long)deg[v], have);
+        }
+    }
+    *labels = static_cast<uint32_t *>(malloc(sizeof(uint32_t) * std::max<uint64_t>(n, 1)));
+    if (!*labels) {
+        drop();
+        return fail(SGE_OOM, "host allocation of %llu labels failed", (unsigned long long)n);
+    }
+    memcpy(*labels, lab.data(), sizeof(uint32_t) * n);
+    *num_vertices = (uint32_t)n;
+    return SGE_OK;
+}
+
 sge_status sge_save_graph_binary(const char *path, const uint32_t *offsets, const uint32_t *nbrs, uint32_t n) {
     if (!path || !offsets || (!nbrs && offsets[n])) return fail(SGE_BAD_INPUT, "sge_save_graph_binary: null argument");
     FILE *f = fopen(path, "wb");

@@ -46,6 +46,8 @@ typedef std::array<uint8_t, SGE_MAX_K> Perm;
 struct Pattern {
     uint32_t k = 0, m = 0;
     uint32_t adj[SGE_MAX_K] = {};
+    uint32_t label[SGE_MAX_K] = {};  // vertex labels (all 0 when unlabeled)
+    bool labeled = false;
     int deg(uint32_t u) const { return __builtin_popcount(adj[u]); }
     bool edge(uint32_t a, uint32_t b) const { return (adj[a] >> b) & 1u; }
 };
@@ -98,7 +100,7 @@ bool automorphisms(const Pattern &p, std::vector<Perm> &out, size_t limit) {
         bool placed = false;
         for (uint32_t c = cand_stack[i]; c < p.k; ++c) {
             if ((used >> c) & 1u) continue;
-            if (p.deg(c) != p.deg(i)) continue;
+            if (p.deg(c) != p.deg(i) || p.label[c] != p.label[i]) continue;
             bool ok = true;
             for (int j = 0; j < i && ok; ++j)
                 if (p.edge(i, j) != p.edge(c, map[j])) ok = false;
@@ -239,6 +241,7 @@ bool build_blob(const Pattern &p, const uint32_t *order, const std::vector<std::
     b.join_style = join_style;
     b.aut_size = aut_size;
     b.single_bag = single_bag ? 1u : 0u;
+    b.labeled = p.labeled ? 1u : 0u;
     b.count_multiplier = single_bag ? aut_size : 1;
     b.num_restrictions = (uint32_t)restr.size();
     uint32_t lvl[SGE_MAX_K];
@@ -276,6 +279,7 @@ bool build_blob(const Pattern &p, const uint32_t *order, const std::vector<std::
             // intra-tail restrictions totally order the tail.
             for (uint32_t i = ne + 1; i < k; ++i) {
                 if (b.parents[i] != b.parents[ne]) return false;
+                if (p.label[order[i]] != p.label[order[ne]]) return false;  // one candidate set
                 if ((b.lower[i] & ~tail_mask_lv) != (b.lower[ne] & ~tail_mask_lv)) return false;
                 if ((b.upper[i] & ~tail_mask_lv) != (b.upper[ne] & ~tail_mask_lv)) return false;
             }
@@ -467,6 +471,12 @@ static sge_status collect_candidates(uint32_t k, uint32_t m, const uint32_t *edg
     if (opts) o = *opts;
     if (o.max_tail == 0 || o.max_tail > SGE_MAX_TAIL) o.max_tail = SGE_MAX_TAIL;
     if (o.join_style > SGE_JOIN_EXPLORATION) return fail(SGE_BAD_INPUT, "unknown join style %u", o.join_style);
+    if (o.vertex_labels) {
+        // labeled matching: only label-preserving automorphisms restrict symmetry
+        if (o.join_style != SGE_JOIN_WCOJ) return fail(SGE_UNSUPPORTED, "labeled plans use the WCOJ join style");
+        p.labeled = true;
+        for (uint32_t u = 0; u < k; ++u) p.label[u] = o.vertex_labels[u];
+    }
     std::vector<Perm> aut;
     if (!automorphisms(p, aut, 1u << 22)) return fail(SGE_UNSUPPORTED, "automorphism group larger than 2^22");
     const bool single = is_single_bag(p);
@@ -652,6 +662,8 @@ sge_status sge_plan_validate(const sge_plan_blob *b) {
     if (b->root_kind > 2) return fail(SGE_BAD_INPUT, "bad root kind");
     if (b->count_multiplier == 0) return fail(SGE_BAD_INPUT, "count_multiplier is 0");
     if (b->choose_wrap > 1) return fail(SGE_BAD_INPUT, "choose_wrap must be 0 or 1");
+    if (b->labeled > 1) return fail(SGE_BAD_INPUT, "labeled must be 0 or 1");
+    if (b->labeled && b->join_style != SGE_JOIN_WCOJ) return fail(SGE_BAD_INPUT, "labeled plans use the WCOJ join style");
     uint32_t seen = 0;
     for (uint32_t i = 0; i < k; ++i) {
         if (b->order[i] >= k || ((seen >> b->order[i]) & 1u)) return fail(SGE_BAD_INPUT, "order is not a permutation");

@@ -55,7 +55,7 @@ class PlanBlob(C.Structure):
         ("num_partitions", u32), ("part_coef", i32 * SGE_MAX_PARTITIONS),
         ("part_nblocks", u32 * SGE_MAX_PARTITIONS), ("part_block", (u32 * SGE_MAX_TAIL) * SGE_MAX_PARTITIONS),
         ("count_multiplier", u64), ("aut_size", u64), ("single_bag", u32), ("num_restrictions", u32),
-        ("est_cost", C.c_double), ("choose_wrap", u32), ("reserved", u32),
+        ("est_cost", C.c_double), ("choose_wrap", u32), ("labeled", u32),
     ]
 
     def summary(self) -> dict:
@@ -74,7 +74,8 @@ class PlanBlob(C.Structure):
 
 class PlanOpts(C.Structure):
     _fields_ = [("join_style", u32), ("use_iep", u32), ("max_tail", u32), ("seed", u64),
-                ("force_order", C.POINTER(u32)), ("symmetry_seq", C.POINTER(u32)), ("root_edge", C.POINTER(u32))]
+                ("force_order", C.POINTER(u32)), ("symmetry_seq", C.POINTER(u32)), ("root_edge", C.POINTER(u32)),
+                ("vertex_labels", C.POINTER(u32))]
 
 
 class CountOpts(C.Structure):
@@ -177,6 +178,9 @@ SIGNATURES = {
     "sge_count_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, u32, u64, u32, _P(PlanBlob), u32, C.c_void_p,
                                     C.c_void_p]),
     "sge_bags_create": (C.c_int, [C.c_void_p, u32, u32, _P(u32), C.c_char_p, u64, _P(C.c_void_p)]),
+    "sge_load_labeled_graph_file": (C.c_int, [C.c_char_p, _P(_P(u32)), _P(_P(u32)), _P(_P(u32)), _P(u32), _P(u64)]),
+    "sge_graph_set_labels": (C.c_int, [C.c_void_p, _P(u32)]),
+    "sge_plan_set_labels": (C.c_int, [C.c_void_p, _P(u32)]),
     "sge_bags_info": (C.c_int, [C.c_void_p, _P(u32), _P(u64), _P(u64), _P(u32), _P(u32)]),
     "sge_bags_destroy": (C.c_int, [C.c_void_p]),
     "sge_plan_use_bags": (C.c_int, [C.c_void_p, C.c_void_p, _P(u32)]),
@@ -238,6 +242,29 @@ class DataGraph:
         n, nnz = u32(), u64()
         _check(lib().sge_load_graph_file(str(path).encode(), C.byref(off), C.byref(nb), C.byref(n), C.byref(nnz)))
         return cls(_take_u32(off, n.value + 1), _take_u32(nb, nnz.value))
+
+    @classmethod
+    def load_labeled(cls, path: str | os.PathLike) -> "tuple[DataGraph, np.ndarray]":
+        """A labeled graph in the reference's "t / v id label degree / e u v"
+        text format (sge_load_labeled_graph_file): the graph and its labels."""
+        off, nb, lab = C.POINTER(u32)(), C.POINTER(u32)(), C.POINTER(u32)()
+        n, nnz = u32(), u64()
+        _check(lib().sge_load_labeled_graph_file(str(path).encode(), C.byref(off), C.byref(nb), C.byref(lab),
+                                                 C.byref(n), C.byref(nnz)))
+        g = cls(_take_u32(off, n.value + 1), _take_u32(nb, nnz.value))
+        return g, _take_u32(lab, n.value)
+
+    def save_labeled_text(self, path: str | os.PathLike, labels) -> None:
+        """The reference's labeled text format (t / v / e lines)."""
+        deg = np.diff(self.offsets)
+        src = np.repeat(np.arange(self.num_vertices, dtype=np.uint32), deg)
+        keep = src < self.nbrs
+        with open(path, "w") as f:
+            f.write(f"t {self.num_vertices} {int(keep.sum())}\n")
+            for v in range(self.num_vertices):
+                f.write(f"v {v} {int(labels[v])} {int(deg[v])}\n")
+            for a, b in zip(src[keep].tolist(), self.nbrs[keep].tolist()):
+                f.write(f"e {a} {b}\n")
 
     @classmethod
     def from_edges(cls, edges: np.ndarray, num_vertices: int, dedup: bool = True) -> "DataGraph":
@@ -338,8 +365,11 @@ def gen_chung_lu(n: int, m: int, gamma: float, max_deg: int = 0, seed: int = 0) 
 
 
 # --------------------------------------------------------------- planner ----
-def _fix(o: "PlanOpts", symmetry_seq, root_edge) -> list:
+def _fix(o: "PlanOpts", symmetry_seq, root_edge, labels=None) -> list:
     keep = []
+    if labels is not None:
+        keep.append(np.ascontiguousarray(labels, dtype=np.uint32))
+        o.vertex_labels = _u32p(keep[-1])
     if symmetry_seq is not None:
         keep.append(np.ascontiguousarray(symmetry_seq, dtype=np.uint32))
         o.symmetry_seq = _u32p(keep[-1])
@@ -351,14 +381,16 @@ def _fix(o: "PlanOpts", symmetry_seq, root_edge) -> list:
 
 def plan(pattern: PatternGraph, graph: "Engine | GraphStats | DataGraph | None" = None, iep: bool = True,
          exploration: bool = False, max_tail: int = SGE_MAX_TAIL, force_order=None, seed: int = 1,
-         symmetry_seq=None, root_edge=None) -> PlanBlob:
+         symmetry_seq=None, root_edge=None, labels=None) -> PlanBlob:
     """Plans a pattern (the host planning half of graph_mining_system).  The
     cost model reads the graph's statistics: pass the Engine, a DataGraph, or
     precomputed GraphStats (None = a generic sparse graph).  symmetry_seq and
     root_edge fix the symmetry restrictions and the root pattern edge of every
-    candidate, so plans agree on any root sample."""
+    candidate, so plans agree on any root sample.  labels (k values) plans
+    labeled matching: count with the same labels (Engine.count(labels=...))
+    on a graph with vertex labels (Engine.set_labels)."""
     o = PlanOpts(JOIN_EXPLORATION if exploration else JOIN_WCOJ, int(iep), max_tail, seed, None)
-    keep = _fix(o, symmetry_seq, root_edge)
+    keep = _fix(o, symmetry_seq, root_edge, labels)
     if force_order is not None:
         keep.append(np.ascontiguousarray(force_order, dtype=np.uint32))
         o.force_order = _u32p(keep[-1])
@@ -419,7 +451,7 @@ def _plan_opts(iep: bool, exploration: bool, max_tail: int, seed: int) -> PlanOp
 
 def candidates(pattern: PatternGraph, stats: "GraphStats | None", iep: bool = True, exploration: bool = False,
                cap: int = 64, max_tail: int = SGE_MAX_TAIL, symmetry_seq=None, root_edge=None,
-               force_order=None) -> list[PlanBlob]:
+               force_order=None, labels=None) -> list[PlanBlob]:
     """Every executable plan of the pattern, cheapest first by the cost model
     (symmetry_seq / root_edge as in plan(); force_order: only that matching
     order, with every tail length and restriction scheme)."""
@@ -427,7 +459,7 @@ def candidates(pattern: PatternGraph, stats: "GraphStats | None", iep: bool = Tr
     n = u32()
     e = pattern.flat()
     o = _plan_opts(iep, exploration, max_tail, 1)
-    keep = _fix(o, symmetry_seq, root_edge)  # (kept alive for the call)
+    keep = _fix(o, symmetry_seq, root_edge, labels)  # (kept alive for the call)
     if force_order is not None:
         keep.append(np.ascontiguousarray(force_order, dtype=np.uint32))
         o.force_order = _u32p(keep[-1])
@@ -579,7 +611,7 @@ class Engine:
               max_level_capacity: int = 0, blocks_per_sm: int = 0, warps_per_block: int = 0, chunk: int = 0,
               root_stride: int = 1, root_offset: int = 0, heavy_threshold: int = 0, hub_bitmaps: bool = True,
               root_max_degree: int = 0, pin_tables: int = 0, tuning: "list[PlanTuning | None] | None" = None,
-              plan_times: bool = False, bags: "list[Bags | None] | None" = None):
+              plan_times: bool = False, bags: "list[Bags | None] | None" = None, labels=None):
         """Counts every plan over the graph in one launch.  Returns (counts,
         instances, stats-dict); counts are the reference's "Number of matches"
         (uint64).  stats=True runs the instrumented kernel (set operations,
@@ -597,7 +629,9 @@ class Engine:
         its roots took (sge_count_plan_times; instances are then not read).
         bags gives each plan the bag relations its tail levels read
         (sge_plan_use_bags; None = intersect adjacency lists);
-        stats["bag_levels"] then lists, per plan, the tail levels that did."""
+        stats["bag_levels"] then lists, per plan, the tail levels that did.
+        labels gives each labeled plan its k pattern labels (sge_plan_set_labels;
+        the graph's come from set_labels)."""
         handles = []
         bag_levels = []
         try:
@@ -607,6 +641,9 @@ class Engine:
                 handles.append(ph)
                 if tuning is not None and tuning[i] is not None:
                     _check(lib().sge_plan_set_tuning(ph, C.byref(tuning[i])))
+                if labels is not None and labels[i] is not None:
+                    la = np.ascontiguousarray(labels[i], np.uint32)
+                    _check(lib().sge_plan_set_labels(ph, _u32p(la)))
                 if bags is not None and bags[i] is not None:
                     lv = u32()
                     _check(lib().sge_plan_use_bags(ph, bags[i]._h, C.byref(lv)))
@@ -634,6 +671,16 @@ class Engine:
         finally:
             for h in handles:
                 lib().sge_plan_destroy(h)
+
+    def set_labels(self, labels) -> None:
+        """One label per data vertex (sge_graph_set_labels); None removes them."""
+        if labels is None:
+            _check(lib().sge_graph_set_labels(self._h, None))
+            return
+        la = np.ascontiguousarray(labels, np.uint32)
+        if la.size != self.info()["num_vertices"]:
+            raise SgeError(1, f"{la.size} labels for {self.info()['num_vertices']} vertices")
+        _check(lib().sge_graph_set_labels(self._h, _u32p(la)))
 
     def bags(self, pattern: PatternGraph, text: str, max_rows: int = 0) -> "Bags":
         """Bag relations of the decomposition in `text` on this graph
