@@ -13,6 +13,9 @@
 // row per instance in the row format of the reference's storeMatches
 // (matching/join.cpp:1703-1711: the row count, then the ids of each row
 // followed by a space).  The reference itself never writes this set.
+// Labeled graphs in the reference's "t / v id label degree / e u v" text
+// format are recognised by their leading 't' (data and query alike): a
+// labeled query on a labeled data graph is counted with labels.
 // Planning runs on the host; the join runs on the GPU through libsge.
 #include <chrono>
 #include <cstdio>
@@ -27,6 +30,13 @@
 #include "sge.h"
 
 namespace {
+
+// A file in the labeled text format starts with 't'.
+bool is_labeled_file(const std::string &path) {
+    std::ifstream f(path);
+    char c = 0;
+    return f && (f >> c) && c == 't';
+}
 
 struct Args {
     std::string q, d, r, batch, plan;
@@ -96,14 +106,17 @@ int main(int argc, char **argv) {
     } else {
         queries.push_back(a.q);
     }
-    uint32_t *off = nullptr, *nb = nullptr, n = 0;
+    uint32_t *off = nullptr, *nb = nullptr, *glab = nullptr, n = 0;
     uint64_t nnz = 0;
-    if (sge_load_graph_file(a.d.c_str(), &off, &nb, &n, &nnz) != SGE_OK) {
+    const bool data_labeled = is_labeled_file(a.d);
+    if ((data_labeled ? sge_load_labeled_graph_file(a.d.c_str(), &off, &nb, &glab, &n, &nnz)
+                      : sge_load_graph_file(a.d.c_str(), &off, &nb, &n, &nnz)) != SGE_OK) {
         std::cout << sge_last_error() << std::endl;
         return 1;
     }
     sge_graph *g = nullptr;
-    if (sge_graph_create(off, nb, n, nnz, a.device, &g) != SGE_OK) {
+    if (sge_graph_create(off, nb, n, nnz, a.device, &g) != SGE_OK ||
+        (data_labeled && sge_graph_set_labels(g, glab) != SGE_OK)) {
         std::cout << "error: " << sge_last_error() << std::endl;
         return 1;
     }
@@ -113,6 +126,7 @@ int main(int argc, char **argv) {
     std::vector<std::vector<uint32_t>> pedges;
     std::vector<uint32_t> pk;
     std::vector<uint32_t> nbags;
+    std::vector<char> qlabeled;
     sge_bags *bags = nullptr;
     sge_graph_stats gst{};
     if (!plan_text.empty() && sge_graph_stats_compute(off, nb, n, &gst) != SGE_OK) {
@@ -120,8 +134,32 @@ int main(int argc, char **argv) {
         return 1;
     }
     for (auto &qp : queries) {
-        uint32_t k, m, edges[2 * SGE_MAX_K * SGE_MAX_K];
-        if (sge_load_pattern_file(qp.c_str(), &k, &m, edges) != SGE_OK) {
+        uint32_t k = 0, m = 0, edges[2 * SGE_MAX_K * SGE_MAX_K];
+        uint32_t qlab[SGE_MAX_K] = {};
+        const bool query_labeled = is_labeled_file(qp);
+        if (query_labeled) {
+            // a labeled query: its CSR back to an edge list, plus its labels
+            uint32_t *qo = nullptr, *qn = nullptr, *ql = nullptr, qv = 0;
+            uint64_t qnnz = 0;
+            if (sge_load_labeled_graph_file(qp.c_str(), &qo, &qn, &ql, &qv, &qnnz) != SGE_OK) {
+                std::cout << sge_last_error() << std::endl;
+                return 1;
+            }
+            if (qv > SGE_MAX_K || !data_labeled) {
+                std::cout << "error: " << (qv > SGE_MAX_K ? "query has too many vertices" : "labeled query on an unlabeled data graph")
+                          << std::endl;
+                return 1;
+            }
+            k = qv;
+            for (uint32_t u = 0; u < qv; ++u) {
+                qlab[u] = ql[u];
+                for (uint32_t e = qo[u]; e < qo[u + 1]; ++e)
+                    if (qn[e] > u) { edges[2 * m] = u; edges[2 * m + 1] = qn[e]; ++m; }
+            }
+            sge_free_host(qo);
+            sge_free_host(qn);
+            sge_free_host(ql);
+        } else if (sge_load_pattern_file(qp.c_str(), &k, &m, edges) != SGE_OK) {
             std::cout << sge_last_error() << std::endl;
             return 1;
         }
@@ -130,6 +168,7 @@ int main(int argc, char **argv) {
         po.use_iep = a.iep ? 1u : 0u;
         po.max_tail = SGE_MAX_TAIL;
         po.seed = a.seed;
+        if (query_labeled) po.vertex_labels = qlab;
         sge_plan_blob b;
         uint32_t nb_plan = 0;
         const sge_status ps = plan_text.empty()
@@ -140,7 +179,7 @@ int main(int argc, char **argv) {
             return 1;
         }
         sge_plan *p = nullptr;
-        if (sge_plan_create(&b, &p) != SGE_OK) {
+        if (sge_plan_create(&b, &p) != SGE_OK || (query_labeled && sge_plan_set_labels(p, qlab) != SGE_OK)) {
             std::cout << "error: " << sge_last_error() << std::endl;
             return 1;
         }
@@ -153,6 +192,7 @@ int main(int argc, char **argv) {
             }
         }
         nbags.push_back(plan_text.empty() ? (b.single_bag ? 1u : 2u) : nb_plan);
+        qlabeled.push_back(query_labeled ? 1 : 0);
         blobs.push_back(b);
         plans.push_back(p);
         pedges.emplace_back(edges, edges + 2 * m);
@@ -198,6 +238,10 @@ int main(int argc, char **argv) {
     out << "GPU time (ms): " << st.kernel_ms << std::endl;
     if (!a.r.empty()) {
         for (size_t i = 0; i < plans.size(); ++i) {
+            if (qlabeled[i]) {  // the instance set is written for unlabeled queries only
+                out << "Matches not written (labeled query)" << std::endl;
+                continue;
+            }
             const uint32_t k = pk[i], m = (uint32_t)(pedges[i].size() / 2);
             sge_plan_opts po{};
             po.use_iep = 0;
@@ -232,5 +276,6 @@ int main(int argc, char **argv) {
     sge_graph_destroy(g);
     sge_free_host(off);
     sge_free_host(nb);
+    sge_free_host(glab);
     return 0;
 }

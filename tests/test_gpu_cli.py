@@ -87,3 +87,22 @@ def test_cli_runs_the_reference_plan(sge, patterns, tmp_path, bags):
     assert re.search(rf"Number of matches: {r['count']}\b", out.stdout), out.stdout
     assert "num bags: 3" in out.stdout
     assert ("bag relations:" in out.stdout) == bags
+
+
+def test_cli_labeled_files(sge, oracle, graphs, tmp_path):
+    """Data and query in the reference's labeled text format: the count is
+    the labeled one (brute force)."""
+    import numpy as np
+    g = graphs("chunglu_n380")
+    glab = np.random.default_rng(4).integers(0, 2, g.num_vertices).astype(np.uint32)
+    d = tmp_path / "d.lg"
+    g.save_labeled_text(d, glab)
+    q = tmp_path / "q.lg"
+    q.write_text("t 4 4\nv 0 0 2\nv 1 1 2\nv 2 0 2\nv 3 1 2\ne 0 1\ne 1 2\ne 2 3\ne 0 3\n")  # a 4-cycle, labels 0,1,0,1
+    out = subprocess.run([str(PKG / "_build" / "graph_mining_system"), "-q", str(q), "-d", str(d), "-u"],
+                         capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    e = [(0, 1), (1, 2), (2, 3), (0, 3)]
+    emb = oracle.bruteforce_embeddings_labeled(g.offsets, g.nbrs, 4, e, [0, 1, 0, 1], glab)
+    inst = emb // oracle.aut_size_labeled(4, e, [0, 1, 0, 1])
+    assert re.search(rf"Number of matches: {inst}\b", out.stdout), (inst, out.stdout)
