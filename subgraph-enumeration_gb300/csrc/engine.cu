@@ -860,7 +860,6 @@ __device__ __forceinline__ uint32_t td_probe_cost(const TailDesc &D, const LeafS
 }
 
 __device__ __forceinline__ bool td_excluded(const TailDesc &D, const LeafState &L, uint32_t l, uint32_t y) {
-    if (D.vlab && __ldg(D.vlab + y) != D.lab) return true;
     bool ex = false;
     for (uint32_t e = 0; e < D.nex; ++e) ex |= D.exv[e] == y;
     if (D.ex_slots & 1u) ex |= L.cm[l][0] == y;
@@ -876,6 +875,7 @@ __device__ __forceinline__ bool td_member(const TailDesc &D, const LeafState &L,
     if ((b.has_lo && y <= b.lo) || (b.has_hi && y >= b.hi)) return false;
     for (uint32_t q = 0; q < D.nsrc; ++q)
         if (!td_has(D, L, W, c, q, l, y)) return false;
+    if (D.vlab && __ldg(D.vlab + y) != D.lab) return false;  // labeled plans
     return !td_excluded(D, L, l, y);
 }
 
@@ -1066,6 +1066,7 @@ __device__ unsigned long long leaf_chunk(const DevPlan &P, WarpState &W, Ctx<STA
             for (uint32_t q = 0; q < ns && ok; ++q)
                 if (q != bq) ok = td_has(D, L, W, c, q, l, y);
             if (ok) ok = !td_excluded(D, L, l, y);
+            if (ok && P.vlab) ok = __ldg(P.vlab + y) == D.lab;
             if (!ok) continue;
             if (P.tail_mode == SGE_TAIL_SINGLE) {
                 ++single;
@@ -1265,7 +1266,7 @@ __device__ bool pair_level(const DevPlan &P, WarpState &W, Ctx<STATS> &c, uint32
         const uint32_t idx = b0 + lane;
         bool valid = idx < n;
         const uint32_t xv = valid ? lst[idx] : 0u;
-        if (valid) valid = !rejected(P, W, a, xv);
+        if (valid) valid = !excluded(P, W, a, xv);  // (labeled plans take no pair step)
         const uint32_t bal = __ballot_sync(FULL_MASK, valid);
         const uint32_t nc = __popc(bal);
         if (valid) S.x[__popc(bal & ((1u << lane) - 1u))] = xv;
