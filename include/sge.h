@@ -398,7 +398,7 @@ sge_status sge_plan_set_tuning(sge_plan *p, const sge_plan_tuning *t);
  * only to data vertices of label labels[u]: the root edge's ends and every
  * enumerated candidate are checked, and tail levels are counted by a scan
  * that checks labels (not by range size).  WCOJ plans only; bag relations,
- * sge_enumerate and sge_count_noalloc take unlabeled plans. */
+ * sge_enumerate, sge_count_host and sge_count_noalloc take unlabeled plans. */
 sge_status sge_graph_set_labels(sge_graph *g, const uint32_t *labels);
 sge_status sge_plan_set_labels(sge_plan *p, const uint32_t *labels);
 
