@@ -102,3 +102,15 @@ def test_every_recorded_plan_runs_on_the_gpu(sge, patterns, ca, ref_plans, golde
         counts, _, _ = eng.count(plans)       # one batched launch of all 214 imported plans
     bad = [(r["pattern"], r["mode"], c, r["count"]) for r, c in zip(rows, counts) if c != expected(r, golden_default)]
     assert not bad, bad[:5]
+
+
+def test_import_counts_other_bags_own_attributes_at_the_leaf(sge):
+    """As sharedJoin, the attributes outside the global bag are counted at the
+    leaf: with -u the imported plan's tail is all of them (here 0 and 5, the
+    own vertices of the triangle bags), without -u a single level."""
+    p = sge.PatternGraph.from_edges(6, [(0, 1), (0, 2), (1, 2), (3, 4), (3, 5), (4, 5), (1, 3), (2, 4)])
+    text = "num bags: 5\n1,0,2\n3,1,2\n3,4,2\n3,4,5\n3,4,1,2\n"
+    b, nb = sge.plan_from_reference(p, text, None, iep=True)
+    assert nb == 5 and b.tail_len == 2 and sorted(b.order[4:6]) == [0, 5] and b.tail_mode == 3
+    b1, _ = sge.plan_from_reference(p, text, None, iep=False)
+    assert b1.tail_len == 1 and list(b1.order[:4]) == [3, 4, 1, 2]
