@@ -46,3 +46,19 @@ def test_gpu_matches_reference_on_downscaled_rmat(sge, patterns, gold, graph):
                 counts, _, _ = eng.count(plans)
                 bad = [(r["pattern"], c, r["count"]) for r, c in zip(rows, counts) if c != r["count"]]
                 assert not bad, (iep, expl, bad)
+
+
+def test_imported_decompositions_on_the_oracle(sge, oracle, patterns, gold):
+    """The decompositions the reference printed on R-MAT 2^14 (its quick
+    multi-bag rows), imported as the reference's plan and run by the CPU
+    oracle, give the reference's counts."""
+    g = graph_of(sge, gold, "rmat_s14")
+    rows = [r for r in gold["results"] if r["graph"] == "rmat_s14" and r["rc"] == 0 and r.get("plan")
+            and r["num_bags"] > 1 and r["seconds"] < 6]
+    assert len(rows) >= 3
+    for r in rows:
+        p = pattern_of(sge, patterns, r["pattern"])
+        b, nb = sge.plan_from_reference(p, r["plan"], g, iep=True)
+        assert nb == r["num_bags"]
+        inst, _ = oracle.count_plan(g.offsets, g.nbrs, b, threads=0)
+        assert inst * b.count_multiplier == r["count"], r["pattern"]
