@@ -113,3 +113,16 @@ def test_labeled_plans_need_labels(sge, graphs):
             eng.count([b])                           # the plan has none
         assert e.value.status_name == "BAD_INPUT"
         assert eng.count([b], labels=[[0, 1, 1]])[0] == [0]   # no vertex has label 1
+
+
+def test_labeled_brute_force_partitions_the_embeddings(sge, oracle, graphs):
+    """Each embedding induces one pattern labeling (its images' labels), so the
+    labeled counts over all 2^k labelings add up to the unlabeled count."""
+    import itertools
+    g = graphs("ca_netscience")
+    glab = np.random.default_rng(2).integers(0, 2, g.num_vertices).astype(np.uint32)
+    for name in ("diamond", "tailed_triangle", "cycle4"):
+        k, e = PATTERNS[name]
+        total = sum(oracle.bruteforce_embeddings_labeled(g.offsets, g.nbrs, k, e, list(lab), glab)
+                    for lab in itertools.product((0, 1), repeat=k))
+        assert total == oracle.bruteforce_embeddings(g.offsets, g.nbrs, k, e), name
